@@ -1,0 +1,104 @@
+"""Extract the reference's own golden values for the fermion hot path into
+reference_goldens.json.
+
+Run in a container where the lehner/gpt sources are mounted (the default
+location is /root/reference; pass another root as argv[1]).  Only numbers
+are extracted -- no code -- from:
+
+  tests/core/checksums.py:11-21          sha256 of a test string (vs hashlib)
+  tests/random/simple.py:17-31           plaquettes of g.qcd.gauge.random
+  tests/random/simple.py:66-127          normal() samples at five coordinates
+  tests/random/simple.py:129-141         rng.choice() results
+  tests/qcd/fermion_operators.py:338-524 Grid operator fingerprints
+"""
+import ast
+import json
+import os
+import re
+import sys
+
+root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+def read(p):
+    with open(os.path.join(root, p)) as f:
+        return f.read()
+
+
+def lit(src, name):
+    """Evaluate the literal assigned to `name` in a reference test file."""
+    tree = ast.parse(src)
+    for node in ast.walk(tree):
+        if isinstance(node, ast.Assign) and any(isinstance(t, ast.Name) and t.id == name for t in node.targets):
+            return node.value
+    raise KeyError(name)
+
+
+def cplx_list(node):
+    return [[complex(ast.literal_eval(e)).real, complex(ast.literal_eval(e)).imag] for e in node.elts]
+
+
+out = {"source": "lehner/gpt test files (paths relative to the project root)"}
+
+simple = read("tests/random/simple.py")
+m = re.findall(r"\(grid_\w+, ([0-9e.-]+), ([0-9e.-]+), (\d+)\)", simple)
+out["plaquette"] = {
+    "cite": "tests/random/simple.py:17-31",
+    "seed": "block_seed_string_13",
+    "cases": [
+        {"grid": [8, 4, 4, 4], "tol_sq": float(m[0][0]), "plaquette": float(m[0][1]), "scale": float(m[0][2])},
+        {"grid": [8, 4, 4, 4], "tol_sq": float(m[1][0]), "plaquette": float(m[1][1]), "scale": float(m[1][2]), "single": True},
+        {"grid": [8, 8, 4, 8], "tol_sq": float(m[2][0]), "plaquette": float(m[2][1]), "scale": float(m[2][2])},
+    ],
+}
+refs = re.findall(r"test_sequence_ref = np\.array\(\s*\[([^\]]*)\]", simple)
+out["normal_samples"] = {
+    "cite": "tests/random/simple.py:91-127",
+    "seed": "block_seed_string_13",
+    "grid": [8, 4, 4, 4],
+    "coords": [[0, 0, 0, 0], [2, 0, 0, 0], [0, 2, 0, 0], [1, 3, 1, 3], [3, 2, 1, 0]],
+    "after_0": [float(x) for x in refs[0].replace("\n", " ").split(",") if x.strip()],
+    "after_1000": [float(x) for x in refs[1].replace("\n", " ").split(",") if x.strip()],
+    "tol": 1e-14,
+}
+ch = re.search(r'assert rng\.choice\(\["A", "B", "C"\], 10\) == \[([^\]]*)\]', simple, re.S).group(1)
+ch2 = re.search(r"np\.array\(\[1, 2, 3\]\), 5\) == np\.array\(\[([^\]]*)\]", simple).group(1)
+out["choice"] = {
+    "cite": "tests/random/simple.py:129-141",
+    "abc_10": [x.strip().strip('"') for x in ch.split(",") if x.strip()],
+    "123_5": [int(x) for x in ch2.split(",")],
+}
+cs = read("tests/core/checksums.py")
+out["sha256"] = {"cite": "tests/core/checksums.py:11-21", "input": re.search(r'test = b"([^"]*)"', cs).group(1)}
+
+fo = read("tests/qcd/fermion_operators.py")
+params = {}
+for pname in ["wilson_params", "wilson_clover_params"]:
+    node = lit(fo, pname)
+    params[pname] = {ast.literal_eval(k): ast.literal_eval(v) for k, v in zip(node.keys, node.values)}
+mats = {}
+for mname in ["wilson_matrices", "wilson_clover_matrices"]:
+    node = lit(fo, mname)
+    mats[mname] = {ast.literal_eval(k): cplx_list(v)[0] for k, v in zip(node.keys, node.values)}
+suite = lit(fo, "test_suite")
+mob = {}
+for k, v in zip(suite.keys, suite.values):
+    key = ast.literal_eval(k)
+    if key not in ("mobius", "mobius_axial_mass"):
+        continue
+    d = {ast.literal_eval(kk): vv for kk, vv in zip(v.keys, v.values)}
+    p = {ast.literal_eval(kk): ast.literal_eval(vv) for kk, vv in zip(d["params"].keys, d["params"].values)}
+    mm = {ast.literal_eval(kk): cplx_list(vv)[0] for kk, vv in zip(d["matrices"].keys, d["matrices"].values)}
+    mob[key] = {"params": p, "matrices": mm}
+out["fingerprints"] = {
+    "cite": "tests/qcd/fermion_operators.py:338-524 (procedure 847-908)",
+    "seed": "finger_print",
+    "grid": [8, 8, 8, 16],
+    "rel_tol": 1e-13,
+    "wilson": {"params": params["wilson_params"], "matrices": mats["wilson_matrices"]},
+    "wilson_clover": {"params": params["wilson_clover_params"], "matrices": mats["wilson_clover_matrices"]},
+    **mob,
+}
+with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json"), "w") as f:
+    json.dump(out, f, indent=1)
+print("wrote reference_goldens.json")

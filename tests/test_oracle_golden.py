@@ -1,0 +1,152 @@
+"""Pin the CPU oracle to the reference's own golden values.
+
+The golden numbers live in tests/golden/reference_goldens.json (extracted from
+the lehner/gpt test files by tests/golden/make_reference_goldens.py).  Passing
+these tests means the oracle reproduces gpt's RNG bit-exactly and Grid's
+Wilson, Wilson-clover and Mobius operators to the reference's fingerprint
+tolerance (relative 1e-13, tests/qcd/fermion_operators.py:527).
+"""
+import hashlib
+import json
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import oracle as o
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+
+
+def test_sha256_matches_hashlib():
+    data = GOLD["sha256"]["input"].encode()
+    assert o.sha256_words(data) == list(struct.unpack(">8I", hashlib.sha256(data).digest()))
+    for n in [0, 1, 55, 56, 63, 64, 65, 119, 120, 200]:
+        d = bytes((i * 7 + 3) % 256 for i in range(n))
+        assert o.sha256_words(d) == list(struct.unpack(">8I", hashlib.sha256(d).digest()))
+
+
+def test_plaquette_goldens():
+    # tests/random/simple.py:17-31: one engine, three grids in sequence
+    rng = o.random(GOLD["plaquette"]["seed"])
+    for case in GOLD["plaquette"]["cases"]:
+        g = o.grid(case["grid"])
+        U = rng.gauge(g, case["scale"])
+        if case.get("single"):
+            U = U.astype(np.complex64).astype(np.complex128)
+        p = o.plaquette(U, g.dims)
+        assert abs(p - case["plaquette"]) ** 2 < case["tol_sq"]
+        for mu in range(4):
+            dev = np.einsum("vji,vjk->vik", U[mu].conj(), U[mu]) - np.eye(3)
+            assert np.linalg.norm(dev) ** 2 / np.linalg.norm(U[mu]) ** 2 < case["tol_sq"]
+
+
+def _pick(v, dims, coords):
+    v = v[:, 0].reshape(dims[::-1])
+    return np.array([v[tuple(c[::-1])].real for c in coords])
+
+
+def test_normal_samples_and_choice():
+    # tests/random/simple.py:38-141: a fresh engine draws zn/normal scalars,
+    # then samples a complex field twice (second time after 1000 refills)
+    ns = GOLD["normal_samples"]
+    rng = o.random(ns["seed"])
+    for _ in range(10000):
+        rng.zn()
+    for _ in range(10000):
+        rng.zn(n=3)
+    for _ in range(10000):
+        rng.normal()
+    g = o.grid(ns["grid"])
+    v = rng.normal(g)
+    assert np.linalg.norm(_pick(v, ns["grid"], ns["coords"]) - ns["after_0"]) < ns["tol"]
+    for _ in range(1000):
+        v = rng.normal(g)
+    assert np.linalg.norm(_pick(v, ns["grid"], ns["coords"]) - ns["after_1000"]) < ns["tol"]
+    assert rng.choice(["A", "B", "C"], 10) == GOLD["choice"]["abc_10"]
+    assert list(rng.choice(np.array([1, 2, 3]), 5)) == GOLD["choice"]["123_5"]
+
+
+def _fingerprint_fields(dims, Ls=None):
+    fp = GOLD["fingerprints"]
+    rng = o.random(fp["seed"])
+    g4 = o.grid(dims)
+    U = rng.gauge(g4)
+    f = {"U": U}
+    if Ls is not None:
+        g5 = o.grid([Ls] + dims)
+        f["src5"], f["dst5"] = rng.spincolor(g5), rng.spincolor(g5)
+    f["src4"], f["dst4"] = rng.spincolor(g4), rng.spincolor(g4)
+    return f
+
+
+@pytest.mark.parametrize("name", ["wilson", "wilson_clover"])
+def test_wilson_clover_fingerprints(name):
+    fp = GOLD["fingerprints"]
+    dims = fp["grid"]
+    case = fp[name]
+    f = _fingerprint_fields(dims)
+    op = o.wilson_clover(f["U"], dims, **case["params"])
+    for tag, ref in case["matrices"].items():
+        opname = {"": "M", ".Mdiag": "Mdiag"}[tag]
+        X = o.inner(f["dst4"], op.apply(opname, f["src4"]))
+        assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (name, tag, X)
+
+
+@pytest.mark.parametrize("name", ["mobius", "mobius_axial_mass"])
+def test_mobius_fingerprints(name):
+    fp = GOLD["fingerprints"]
+    dims = fp["grid"]
+    case = fp[name]
+    p = case["params"]
+    f = _fingerprint_fields(dims, Ls=p["Ls"])
+    op = o.mobius(f["U"], dims, **p)
+    for tag, ref in case["matrices"].items():
+        if tag == ".ImportPhysicalFermionSource":
+            X = o.inner(f["dst5"], op.import_physical_source(f["src4"]))
+        else:
+            X = o.inner(f["dst5"], op.apply({"": "M", ".Mdiag": "Mdiag"}[tag], f["src5"]))
+        assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (name, tag, X)
+
+
+def test_eo_decomposition_identities():
+    # M restricted to a parity equals Mooee + Meooe (fermion_operators.py:677-695)
+    dims = [4, 4, 4, 8]
+    U = o.synthetic_gauge(dims, 0.5, 7)
+    rng = np.random.default_rng(1)
+    src = rng.standard_normal((np.prod(dims), 4, 3)) + 1j * rng.standard_normal((np.prod(dims), 4, 3))
+    for op in [o.wilson_clover(U, dims, mass=0.1, csw_r=1.0, csw_t=1.0),
+               o.mobius(U, dims, Ls=4, b=1.5, c=0.5, M5=1.8, mass=0.05)]:
+        s = src if op.n5 == 1 else np.repeat(src[:, None], op.n5, axis=1) * (1 + np.arange(op.n5))[None, :, None, None]
+        full = op.apply("M", s)
+        for p in [o.EVEN, o.ODD]:
+            part = op.apply("Meooe", s, p) + op.apply("Mooee", s, p)
+            mask = o.parity_of_sites(dims) == p
+            assert np.linalg.norm((full - part)[mask]) / np.linalg.norm(full[mask]) < 1e-14
+        # adjoint consistency <a, M b> = conj(<b, M^+ a>)
+        a = np.roll(s, 3)
+        for m, md in [("M", "Mdag"), ("Dhop", "DhopDag")]:
+            x1 = o.inner(a, op.apply(m, s))
+            x2 = np.conj(o.inner(s, op.apply(md, a)))
+            assert abs(x1 - x2) / abs(x1) < 1e-13
+        # inverse consistency of Mooee
+        for p in [o.EVEN, o.ODD]:
+            y = op.apply("MooeeInv", op.apply("Mooee", s, p), p)
+            mask = o.parity_of_sites(dims) == p
+            assert np.linalg.norm((y - s)[mask]) / np.linalg.norm(s[mask]) < 1e-13
+
+
+def test_oracle_solvers_true_residual():
+    dims = [4, 4, 4, 8]
+    U = o.synthetic_gauge(dims, 0.5, 3)
+    rng = np.random.default_rng(2)
+    op = o.wilson_clover(U, dims, mass=0.1, csw_r=1.0, csw_t=1.0, with_single=True)
+    src = rng.standard_normal((op.V, 4, 3)) + 1j * rng.standard_normal((op.V, 4, 3))
+    x, it, res = op.eo2ne_cg(src, 1e-10, 1000)
+    assert it > 0
+    r = src - op.apply("M", x)
+    assert np.sqrt(o.norm2(r) / o.norm2(src)) < 1e-8
+    x2, it2, nout, tres = op.defect_correcting(src, 1e-10, 20, 1e-5, 1000)
+    assert tres < 1e-10
+    assert np.sqrt(o.norm2(x - x2) / o.norm2(x)) < 1e-8
