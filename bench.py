@@ -1,0 +1,414 @@
+#!/usr/bin/env python3
+"""Benchmark of the fermion-matrix hot path on GB300.
+
+Workload (the reference's second configuration): Wilson-clover fermion on a
+32^4 lattice, gauge links exp(i*0.3*H) with H Hermitian traceless and
+complex-Gaussian entries (seeded), mass 0.05, csw_r = csw_t = 1.0, boundary
+phases [1,1,1,-1], one complex-Gaussian source.  Synthetic data (there is no
+dataset involved).
+
+One step = one propagator solve to true FP64 residual 1e-10 with
+defect_correcting(mixed_precision(preconditioned(eo2_ne, cg(1e-5)), single,
+double), eps=1e-10) -- the mixed method.  `value` = mixed solves/s with the
+source resident in HBM; `e2e` = the same through the public API from pinned
+host memory (source H2D and solution D2H inside the timed region).  The plain
+FP64 eo2_ne CG (eps 1e-10) is measured beside it.  Inputs (gauge field
+604 MB, clover 1.2 GB, source 201 MB FP64) are larger than the 129 MB L2, so
+no L2 flush is needed between steps.
+
+--impl reference runs the CPU restatement of the same solve (the reference's
+Grid CPU operator cannot be built here) on all host cores: each step is a
+bounded sample of inner CG iterations and outer residuals, scaled to solves/s
+with the iteration counts of one full CPU solve done during warm-up.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Dslash HBM GB/s; CG solves/s at FP64 residual 1e-10 (mixed vs plain); p99 ms"
+CFG = dict(dims=[32, 32, 32, 32], gauge_eps=0.3, gauge_seed=2024, src_seed=7, mass=0.05, csw=1.0,
+           phases=[1.0, 1.0, 1.0, -1.0], tol=1e-10, inner_tol=1e-5)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbf", choices=["gbf", "reference"])
+    ap.add_argument("--dims", type=str, default=None, help="override lattice, e.g. 16,16,16,16 (tests only)")
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(dims):
+    return {
+        "workload": f"wilson_clover {'x'.join(map(str, dims))} gauge exp(i*{CFG['gauge_eps']}*H) mass {CFG['mass']} "
+                    f"csw {CFG['csw']} bc [1,1,1,-1], 1 gaussian source, eo2_ne CG: mixed FP32-inner (tol "
+                    f"{CFG['inner_tol']}) + FP64 defect correction to true residual {CFG['tol']}",
+        "lattice": dims,
+        "precision": "FP32 inner / FP64 outer (value), FP64 plain alongside",
+        "l2_policy": "inputs larger than L2 (gauge 604 MB, clover 1.2 GB, FP64 source 201 MB); no flush",
+        "parallelism": "replicas (one independent solve stream per GPU)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement timing (oracle port) -- bounded samples
+# ---------------------------------------------------------------------------
+def cpu_sample_rates(op_o, src, n1=2, n2=8):
+    """Seconds per single-precision eo2_ne CG iteration and per FP64 M."""
+    t0 = time.perf_counter()
+    op_o.eo2ne_cg_single(src, 0.0, n1)
+    t1 = time.perf_counter()
+    op_o.eo2ne_cg_single(src, 0.0, n2)
+    t2 = time.perf_counter()
+    per_iter = ((t2 - t1) - (t1 - t0)) / (n2 - n1)
+    t3 = time.perf_counter()
+    op_o.apply("M", src)
+    t4 = time.perf_counter()
+    return per_iter, t4 - t3, (t2 - t0) + (t4 - t3)
+
+
+def run_reference(args, dims):
+    import oracle as o
+    from gpt_gb300.qcd import gauge as G
+    import gpt_gb300.core as core
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    grid = core.grid.__new__(core.grid)
+    grid.fdimensions, grid.gsites, grid.precision = dims, int(np.prod(dims)), None
+    U = G.random_su3(grid, CFG["gauge_eps"], CFG["gauge_seed"]).U
+    rng = np.random.default_rng(CFG["src_seed"])
+    V = int(np.prod(dims))
+    src = rng.standard_normal((V, 4, 3)) + 1j * rng.standard_normal((V, 4, 3))
+    op = o.wilson_clover(U, dims, mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"],
+                         boundary_phases=CFG["phases"], with_single=True)
+    # warm-up step 1: one full CPU mixed solve gives the iteration counts
+    t0 = time.perf_counter()
+    x, inner_it, n_outer, tres = op.defect_correcting(src, CFG["tol"], 50, CFG["inner_tol"], 100000)
+    full_s = time.perf_counter() - t0
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_sample_rates(op, src)
+    est = []
+    tstart = time.perf_counter()
+    for _ in range(args.steps):
+        per_iter, t_m, _ = cpu_sample_rates(op, src)
+        est.append(inner_it * per_iter + (n_outer + 1) * t_m)
+    wall = time.perf_counter() - tstart
+    sec = statistics.median(est)
+    value = 1.0 / sec
+    cores = o.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+        "data": "synthetic", "config": workload_config(dims),
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"per step: single-precision eo2_ne CG iterations (difference of 8 and 2) and one "
+                                   f"FP64 M, scaled by the iteration counts of one full CPU solve in warm-up "
+                                   f"({inner_it} inner iterations, {n_outer} outer, {full_s:.1f} s, true residual {tres:.2e})"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_full_solve_s": full_s,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gbf(args, dims):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import gpt_gb300 as g
+
+    L = g.load()
+    grid = g.grid(dims, g.double)
+    U = g.qcd.gauge.random_su3(grid, CFG["gauge_eps"], CFG["gauge_seed"] + rank)
+    params = dict(mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"], boundary_phases=CFG["phases"])
+    op = g.qcd.fermion.wilson_clover(U, params)
+    inv = g.algorithms.inverter
+    pc = g.qcd.fermion.preconditioner
+    inner_cg = inv.cg({"eps": CFG["inner_tol"], "maxiter": 20000, "iterations_per_graph": 16})
+    dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inner_cg), g.single, g.double),
+                               eps=CFG["tol"], maxiter=100)
+    solver = dc(op)
+    inner_op = dc.inner_inverter.inner_op  # the FP32 operator built by mixed_precision
+    plain_cg = inv.cg({"eps": CFG["tol"], "maxiter": 40000, "iterations_per_graph": 16})
+    plain = inv.preconditioned(pc.eo2_ne(), plain_cg)(op)
+
+    V = grid.gsites
+    rng = np.random.default_rng(CFG["src_seed"] + rank)
+    src_np = rng.standard_normal((V, 4, 3)) + 1j * rng.standard_normal((V, 4, 3))
+    src = op.F_lattice()
+    src[:] = src_np
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- warm-up ----
+    for _ in range(args.warmup):
+        x = solver(src)
+
+    # ---- timed region: K mixed solves, source resident in HBM ----
+    clocks = Clocks(local if "CUDA_VISIBLE_DEVICES" not in os.environ else local)
+    clocks.start()
+    barrier()
+    n0 = L.gbf_launch_count()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for k in range(args.steps):
+        x = solver(src)
+        ev[k + 1].record(stream)
+    barrier()
+    n1 = L.gbf_launch_count()
+    clk = clocks.stop()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[args.steps])
+    t_local = torch.tensor([total_ms], device="cuda")
+    if dist is not None:
+        dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
+    total_ms = float(t_local.item())
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # true residual of the last solve, FP64 on the device
+    r = op.F_lattice()
+    op.M(r, x)
+    g.axpby(r, -1.0, r, 1.0, src)
+    true_res = math.sqrt(g.norm2(r) / g.norm2(src))
+    outer_iters = len(dc.history) - 1
+
+    # inner CG iterations of one mixed solve (running total kept by the cg object)
+    before = inner_cg.total_iterations
+    x = solver(src)
+    inner_iters_per_solve = inner_cg.total_iterations - before
+    ns = g.norm2(src)
+
+    # ---- e2e through the public API from pinned host memory ----
+    h_src = torch.from_numpy(src_np.view(np.float64).reshape(-1)).pin_memory()
+    h_dst = torch.empty(V * 24, dtype=torch.float64).pin_memory()
+    d_nat = torch.empty(V * 24, dtype=torch.float64, device="cuda")
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        d_nat.copy_(h_src, non_blocking=True)
+        lat = op.F_lattice()
+        g._lib.check(L.gbf_field_import(lat.layout.op, d_nat.data_ptr(), lat.ptr, 0, 0, g.core.stream_ptr()))
+        xo = solver(lat)
+        g._lib.check(L.gbf_field_export(xo.layout.op, xo.ptr, d_nat.data_ptr(), 0, 0, g.core.stream_ptr()))
+        h_dst.copy_(d_nat, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    t_e = torch.tensor([e2e_ms], device="cuda")
+    if dist is not None:
+        dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
+    e2e_value = world * e2e_steps / (float(t_e.item()) / 1000.0)
+
+    # ---- plain FP64 eo2_ne CG ----
+    xp = plain(src)  # warm-up (also builds the graph)
+    plain_it = plain_cg.last.iterations
+    barrier()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(args.plain_steps):
+        xp = plain(src)
+    p1.record(stream)
+    barrier()
+    plain_ms = p0.elapsed_time(p1) / args.plain_steps
+    op.M(r, xp)
+    g.axpby(r, -1.0, r, 1.0, src)
+    plain_true = math.sqrt(g.norm2(r) / g.norm2(src))
+
+    # ---- dominant kernel: FP32 hopping kernel inside the inner CG, timed with
+    # CUDA events around every launch (profile-mode solve on the same stream) ----
+    cs = inner_op.F_lattice()
+    g.convert(cs, src, 1.0 / math.sqrt(ns))
+    xd = inner_op.F_lattice()
+    res32 = inner_op._solve_eo2ne_cg(xd, cs, CFG["inner_tol"], 400, 0, 1)
+    d_ms = res32.kernel_ms[0] / max(1, res32.kernel_launches[0])
+    Vh = V // 2
+    link_b = inner_op.link_bytes()
+    spin_b, clov_b = 96, 288
+    # algorithmic bytes per output site, the four launches of one iteration:
+    #   z = G Dhop t, w = p - Dhop z, u = G Dhop^+ w, mmp = w - G Dhop^+ u (+<p,mmp>)
+    per_site = [spin_b + 8 * link_b + clov_b + spin_b,
+                spin_b + 8 * link_b + spin_b + spin_b,
+                spin_b + 8 * link_b + clov_b + spin_b,
+                spin_b + 8 * link_b + clov_b + spin_b + spin_b + spin_b]
+    bytes_per_launch = statistics.mean(per_site) * Vh
+    achieved = bytes_per_launch / (d_ms / 1000.0) / 1e9
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "dslash_fp32_traffic.json")
+    if os.path.exists(tf):
+        t = json.load(open(tf))
+        traffic = t["dram_bytes_per_site"] * Vh
+
+    # FP64 hopping kernel (plain method), same profile mode
+    res64 = op._solve_eo2ne_cg(op.F_lattice(), src, CFG["tol"], 50, 0, 1)
+    d64_ms = res64.kernel_ms[0] / max(1, res64.kernel_launches[0])
+    per_site64 = statistics.mean([192 + 8 * 144 + 576 + 192, 192 + 8 * 144 + 192 + 192,
+                                  192 + 8 * 144 + 576 + 192, 192 + 8 * 144 + 576 + 3 * 192])
+    fp64_gbs = per_site64 * Vh / (d64_ms / 1000.0) / 1e9
+    fp64_gflops = (1320 + 288 * 0.75 * 4 / 4) * Vh / (d64_ms / 1000.0) / 1e9
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+        return 0
+
+    # ---- CPU baseline (oracle port), rank 0 at N = 1 only ----
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        import oracle as o
+
+        op_o = o.wilson_clover(U.U, dims, mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"],
+                               boundary_phases=CFG["phases"], with_single=True)
+        per_iter, t_m, spent = cpu_sample_rates(op_o, src_np)
+        sec = inner_iters_per_solve * per_iter + (outer_iters + 1) * t_m
+        cpu = {"value": 1.0 / sec, "unit": "solves/s", "cores": o.num_threads(), "kind": "port",
+               "sample": f"single-precision eo2_ne CG iterations (difference of 8 and 2) and one FP64 M on the host, "
+                         f"scaled by this solve's {inner_iters_per_solve} inner iterations and {outer_iters} outer "
+                         f"corrections ({spent:.1f} s of CPU work)"}
+        del op_o
+
+    p = sorted(step_ms)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 inner / f64 outer",
+        "data": "synthetic",
+        "config": workload_config(dims),
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": V * 12 * 16,
+                "d2h_bytes_per_step": V * 12 * 16},
+        "gpu_launches": int(n1 - n0),
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": "dslash_kernel<FP32 spinor, 12-real links, clover epilogue>",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": d_ms},
+        "cpu_baseline": cpu,
+        "p50_ms": p[len(p) // 2],
+        "p99_ms": p[min(len(p) - 1, int(math.ceil(0.99 * len(p))) - 1)],
+        "mixed": {"solves_per_s": value, "true_residual": true_res, "outer_corrections": outer_iters,
+                  "inner_cg_iterations": inner_iters_per_solve},
+        "plain_fp64": {"solves_per_s": world * 1000.0 / plain_ms, "ms_per_solve": plain_ms, "cg_iterations": plain_it,
+                       "true_residual": plain_true},
+        "mixed_over_plain": (value / world) / (1000.0 / plain_ms),
+        "dslash_fp32": {"hbm_gbs": achieved, "avg_launch_ms": d_ms},
+        "dslash_fp64": {"algorithmic_gbs": fp64_gbs, "avg_launch_ms": d64_ms, "gflops_model_1320_per_site": 1320 * Vh / (d64_ms / 1000.0) / 1e9},
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    dims = [int(d) for d in args.dims.split(",")] if args.dims else CFG["dims"]
+    if args.impl == "reference":
+        return run_reference(args, dims)
+    return run_gbf(args, dims)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

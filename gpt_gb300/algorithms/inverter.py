@@ -1,0 +1,135 @@
+"""Krylov inverters of the hot path: cg, preconditioned, defect_correcting,
+mixed_precision (lib/gpt/algorithms/inverter/cg.py:24-117,
+preconditioned.py:24-54, defect_correcting.py:23-142, mixed_precision.py:23-32).
+
+preconditioned(eo2_ne(), cg(...)) on a native fermion operator runs as one
+device-resident solve (prepare, CG in CUDA graphs, reconstruction) through
+gbf_solve_eo2ne_cg.  defect_correcting and mixed_precision compose on the
+host exactly as in the reference, with all vector algebra on the device.
+"""
+import math
+
+from .. import core
+from ..qcd import fermion as _fermion
+
+
+class cg:
+    """gpt.algorithms.inverter.cg(eps, maxiter): CG on the eo2_ne normal
+    equations; convergence when |r|^2 <= eps^2 |b|^2 (cg.py:70, 103)."""
+
+    def __init__(self, params=None, eps=1e-15, maxiter=1000000, fail_if_not_converged=False, iterations_per_graph=0):
+        p = dict(params or {})
+        self.eps = p.get("eps", eps)
+        self.maxiter = p.get("maxiter", maxiter)
+        self.fail_if_not_converged = p.get("fail_if_not_converged", fail_if_not_converged)
+        self.iterations_per_graph = p.get("iterations_per_graph", iterations_per_graph)
+        self.history = []
+        self.last = None
+        self.total_iterations = 0
+
+    def modified(self, **params):
+        d = dict(eps=self.eps, maxiter=self.maxiter, fail_if_not_converged=self.fail_if_not_converged)
+        d.update(params)
+        return cg(d)
+
+    def __call__(self, mat):
+        raise NotImplementedError("cg runs on the device through preconditioned(eo2_ne(), cg(...))")
+
+
+class preconditioned:
+    """M^-1 = L Mpc^-1 R + S (preconditioned.py:28-54)."""
+
+    def __init__(self, preconditioner, inverter, params=None):
+        self.preconditioner = preconditioner
+        self.inverter = inverter
+
+    def __call__(self, op):
+        if not isinstance(self.preconditioner, _fermion.preconditioner.eo2_ne) or not isinstance(self.inverter, cg):
+            raise NotImplementedError("the device path implements preconditioned(eo2_ne(), cg(...))")
+        if not isinstance(op, _fermion.fermion_operator):
+            raise TypeError("expected a native fermion operator")
+        if op.daggered:
+            raise NotImplementedError("solves with the daggered operator are not on this path")
+        inv = self.inverter
+
+        def mat(dst, src):
+            r = op._solve_eo2ne_cg(dst, src, inv.eps, inv.maxiter, inv.iterations_per_graph)
+            inv.last = r
+            inv.history = [None] * r.iterations
+            inv.total_iterations += r.iterations
+            if inv.fail_if_not_converged and not r.converged:
+                raise ValueError("FATAL error: CG not converged")
+
+        def new_dst(src):
+            return op.F_lattice()
+
+        m = _fermion.matrix_operator(mat, inv_mat=op.mat)
+        m._new_dst = new_dst
+        return m
+
+
+class mixed_precision:
+    """Run the inner inverter on op.converted(inner_precision) and convert
+    source and solution (mixed_precision.py:23-32, matrix_operator.py:139-178)."""
+
+    def __init__(self, inverter, inner_precision, outer_precision):
+        self.inverter = inverter
+        self.inner_precision = inner_precision
+        self.outer_precision = outer_precision
+
+    def __call__(self, op):
+        inner_op = op.converted(self.inner_precision)
+        inner = self.inverter(inner_op)
+        self.inner_op = inner_op
+
+        def mat(dst, src):
+            cs = inner_op.F_lattice()
+            core.convert(cs, src)
+            cd = inner(cs)
+            core.convert(dst, cd)
+
+        m = _fermion.matrix_operator(mat, inv_mat=op.mat)
+        m._new_dst = lambda src: op.F_lattice()
+        return m
+
+
+class defect_correcting:
+    """Outer defect correction (defect_correcting.py:85-130): residual
+    s = src - M psi in the outer precision, s normalised by |src|, inner
+    solve, psi += d |src|; stops when max_j |s_j| / |src_j| < eps."""
+
+    def __init__(self, inner_inverter, params=None, eps=1e-15, maxiter=1000000):
+        p = dict(params or {})
+        self.eps = p.get("eps", eps)
+        self.maxiter = p.get("maxiter", maxiter)
+        self.inner_inverter = inner_inverter
+        self.history = []
+
+    def __call__(self, outer_mat):
+        inner_inv_mat = self.inner_inverter(outer_mat)
+        me = self
+
+        def mat(psi, src):
+            n = src.layout.n_rhs
+            ns = core.norm2(src)
+            ns = [ns] if n == 1 else ns
+            ns = [x if x != 0.0 else 1.0 for x in ns]
+            s = src.new()
+            t = src.new()
+            me.history = []
+            for i in range(me.maxiter):
+                outer_mat(t, psi)
+                core.axpby(s, -1.0, t, 1.0, src)
+                nd = core.norm2(s)
+                nd = [nd] if n == 1 else nd
+                eps = max(math.sqrt(nd[j] / ns[j]) for j in range(n))
+                me.history.append(eps)
+                if eps < me.eps:
+                    break
+                core.axpby(s, [1.0 / math.sqrt(x) for x in ns], s)
+                d = inner_inv_mat(s)
+                core.axpby(psi, [math.sqrt(x) for x in ns], d, 1.0, psi)
+
+        m = _fermion.matrix_operator(mat, inv_mat=outer_mat.mat)
+        m._new_dst = lambda src: outer_mat.F_lattice()
+        return m

@@ -1,0 +1,878 @@
+// gbf_api.cu -- the C ABI of include/gbferm.h: operator objects, opcode
+// dispatch onto the kernels, vector algebra and the device-resident
+// eo2_ne-preconditioned CG.
+//
+// Reference interfaces replaced here (paths relative to the gpt project root):
+//   create/update/set_mass/delete/apply  lib/cgpt/lib/operators.cc:34-133
+//   opcode dispatch                       lib/cgpt/lib/operators/unary.h:20-64
+//   Wilson-clover factory                 lib/cgpt/lib/operators/wilson_clover.h:19-71
+//   Mobius factory                        lib/cgpt/lib/operators/mobius.h:34-87
+//   eo2_ne + CG                           lib/gpt/algorithms/preconditioner/schur_complement_two.py:58-152,
+//                                         normal_equation.py:35-65, inverter/cg.py:24-117
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <stdexcept>
+#include "gbf_launch.cuh"
+#include "../../include/gbferm.h"
+
+using namespace gbf;
+
+#include <atomic>
+
+static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+static inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+struct Fail : std::runtime_error {
+  int code;
+  Fail(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                       \
+  do {                                                                                              \
+    cudaError_t e_ = (x);                                                                           \
+    if (e_ != cudaSuccess) throw Fail(GBF_E_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename F> int guarded(F&& f) {
+  try {
+    f();
+    return GBF_OK;
+  } catch (const Fail& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return GBF_E_OOM;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return GBF_E_ARG;
+  }
+}
+
+void* dmalloc(size_t bytes) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Fail(GBF_E_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+  }
+  return p;
+}
+
+// Mobius s-matrix slots (real Ls x Ls per chirality)
+enum { S_A = 0, S_ADAG, S_AINV, S_AINVDAG, S_B, S_BDAG, S_G, S_GDAG, S_COUNT };
+
+}  // namespace
+
+struct gbf_op {
+  std::string name;
+  bool mobius = false;
+  int prec = P64;   // spinor storage precision
+  int LS = L64;     // link storage
+  gbf_params par;
+  Geo g;            // fields of this operator (N5 = Ls * nrhs)
+  Geo g4;           // 4D fields of a mobius operator (N5 = nrhs)
+  double cc[4];
+  double diag = 0;  // 1/(2 kappa) for wilson_clover
+  bool has_clover = false;
+  bool gauge_set = false;
+  void* links = nullptr;
+  void* clov_mem = nullptr;      // clover + inverse, both parities, op precision
+  void* clov[2] = {nullptr, nullptr};
+  void* clov_inv[2] = {nullptr, nullptr};
+  void* smat = nullptr;          // [S_COUNT][2][Ls][Ls] in the arithmetic precision
+  std::vector<double> smat_host; // same in double
+  // workspace
+  void* ws = nullptr;
+  void* tmp[12] = {};
+  double2* partial = nullptr;
+  unsigned* counter = nullptr;
+  CGState* st = nullptr;
+  CGState* hst = nullptr;        // pinned, 2 buffers
+  unsigned* errbits = nullptr;
+  cudaStream_t stream = nullptr; // internal stream for graph capture
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_chk[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph = nullptr;
+  int graph_K = 0;
+
+  size_t half() const { return (size_t)half_bytes(prec, g.N); }
+  size_t half4() const { return (size_t)half_bytes(prec, g4.N); }
+  size_t rb() const { return prec == P64 ? 8 : 4; }
+
+  // ---- site-local operators ----
+  LocalOp none() const { LocalOp l{}; l.kind = LOC_NONE; return l; }
+  LocalOp smat_slot(int s) const {
+    LocalOp l{};
+    l.kind = LOC_SMAT;
+    l.smat = (const char*)smat + (size_t)s * 2 * g.Ls * g.Ls * rb();
+    return l;
+  }
+  LocalOp clover(bool inv) const {
+    LocalOp l{};
+    if (has_clover) {
+      l.kind = LOC_CLOVER;
+      l.clov[0] = inv ? clov_inv[0] : clov[0];
+      l.clov[1] = inv ? clov_inv[1] : clov[1];
+    } else {
+      l.kind = LOC_SCALAR;
+      l.scalar = inv ? 1.0 / diag : diag;
+    }
+    return l;
+  }
+  LocalOp G() const { return mobius ? smat_slot(S_G) : clover(true); }
+  LocalOp Gdag() const { return mobius ? smat_slot(S_GDAG) : clover(true); }
+  LocalOp A(bool dag) const { return mobius ? smat_slot(dag ? S_ADAG : S_A) : clover(false); }
+  LocalOp Ainv(bool dag) const { return mobius ? smat_slot(dag ? S_AINVDAG : S_AINV) : clover(true); }
+  LocalOp B(bool dag) const { return smat_slot(dag ? S_BDAG : S_B); }
+
+  RedArgs red(int fin) const { RedArgs r; r.fin = fin; r.partial = partial; r.counter = counter; r.st = st; return r; }
+
+  // ---- kernel wrappers ----
+  // out(parity p) = c1 * L1(Dhop[^dag](in)) + c2 * L2(X)  [+ reduction]
+  void dslash(cudaStream_t s, int p, bool dag, const void* in, void* out, LocalOp l1, double c1 = 1.0, const void* X = nullptr,
+              double c2 = 0.0, LocalOp l2 = LocalOp{}, int redmode = 0, const void* Y = nullptr, int fin = FIN_STORE,
+              int check_done = 0, const Geo* geo = nullptr) const {
+    DslashArgs a{};
+    a.g = geo ? *geo : g;
+    a.out_parity = p;
+    a.sgn = dag ? 1.f : -1.f;
+    a.in = in;
+    a.out = out;
+    a.links = links;
+    a.l1 = l1;
+    a.l2 = l2;
+    a.c1 = c1;
+    a.c2 = c2;
+    a.X = X;
+    a.red = redmode;
+    a.Y = Y;
+    a.ra = red(fin);
+    a.check_done = check_done;
+    if (l2.kind == LOC_SMAT) throw Fail(GBF_E_ARG, "internal: smat on the X term");
+    CK(launch_dslash(prec, LS, a, s));
+    count_launch();
+  }
+  void local(cudaStream_t s, int p, const void* A_, void* out, LocalOp l, double c1 = 1.0, const void* X = nullptr, double c2 = 0.0,
+             void* W = nullptr, int pre = 0, int redmode = 0, const void* Y = nullptr, int fin = FIN_STORE, int check_done = 0,
+             const Geo* geo = nullptr) const {
+    LocalArgs a{};
+    a.g = geo ? *geo : g;
+    a.parity = p;
+    a.A = A_;
+    a.W = W;
+    a.pre = pre;
+    a.l = l;
+    a.out = out;
+    a.c1 = c1;
+    a.c2 = c2;
+    a.X = X;
+    a.red = redmode;
+    a.Y = Y;
+    a.ra = red(fin);
+    a.check_done = check_done;
+    CK(launch_local(prec, a, s));
+    count_launch();
+  }
+  void cg_update(cudaStream_t s, void* r, const void* mmp, void* x, const void* p) const {
+    CGUpdateArgs a{};
+    a.g = g;
+    a.r = r;
+    a.mmp = mmp;
+    a.x = x;
+    a.p = p;
+    a.ra = red(FIN_BETA);
+    CK(launch_cg_update(prec, a, s));
+    count_launch();
+  }
+};
+
+namespace {
+
+void setup_geo(gbf_op* op) {
+  const gbf_params& p = op->par;
+  Geo& g = op->g;
+  for (int m = 0; m < 4; ++m) g.L[m] = p.dims[m];
+  g.Lh0 = p.dims[0] / 2;
+  long long V = (long long)p.dims[0] * p.dims[1] * p.dims[2] * p.dims[3];
+  g.Vh = (int)(V / 2);
+  g.Ls = op->mobius ? p.Ls : 1;
+  g.nrhs = p.n_rhs;
+  g.N5 = g.Ls * g.nrhs;
+  g.N = (long long)g.Vh * g.N5;
+  for (int m = 0; m < 4; ++m) {
+    g.lam[m] = (float)(-0.5 * op->cc[m]);
+    g.ph_re[m] = (float)p.boundary_phases[2 * m];
+    g.ph_im[m] = (float)p.boundary_phases[2 * m + 1];
+  }
+  op->g4 = g;
+  op->g4.Ls = 1;
+  op->g4.N5 = g.nrhs;
+  op->g4.N = (long long)g.Vh * g.nrhs;
+}
+
+// Cayley s-matrices of the Mobius operator with constant b_s = b, c_s = c
+// (lib/gpt/qcd/fermion/mobius.py:29-46).  With K+ the s-1 -> s hop with the
+// wall term -m+ at (0, Ls-1) and K- the s+1 -> s hop with -m- at (Ls-1, 0):
+//   A = (4-M5)(b + cK) + 1 - K  (Mooee),  B = b + cK,  G = B A^-1.
+void invert_real(int n, std::vector<double> a, std::vector<double>& inv) {
+  inv.assign(n * n, 0.0);
+  for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
+    if (a[piv * n + c] == 0.0) throw Fail(GBF_E_ARG, "singular Mooee (check M5, b, c, masses)");
+    for (int k = 0; k < n; ++k) { std::swap(a[c * n + k], a[piv * n + k]); std::swap(inv[c * n + k], inv[piv * n + k]); }
+    double d = 1.0 / a[c * n + c];
+    for (int k = 0; k < n; ++k) { a[c * n + k] *= d; inv[c * n + k] *= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      double f = a[r * n + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) { a[r * n + k] -= f * a[c * n + k]; inv[r * n + k] -= f * inv[c * n + k]; }
+    }
+  }
+}
+
+void build_smat(gbf_op* op) {
+  const int Ls = op->g.Ls;
+  const gbf_params& p = op->par;
+  const double dg = (4.0 - p.M5) * p.b + 1.0, od = (4.0 - p.M5) * p.c - 1.0;
+  std::vector<double> all((size_t)S_COUNT * 2 * Ls * Ls, 0.0);
+  auto slot = [&](int s, int ch) { return all.data() + ((size_t)s * 2 + ch) * Ls * Ls; };
+  for (int ch = 0; ch < 2; ++ch) {
+    std::vector<double> K(Ls * Ls, 0.0), A(Ls * Ls), B(Ls * Ls), Ai, G(Ls * Ls, 0.0);
+    for (int s = 0; s < Ls; ++s) {
+      if (ch == 0) {
+        if (s >= 1) K[s * Ls + s - 1] = 1.0;
+        else K[Ls - 1] = -p.mass_plus;
+      } else {
+        if (s <= Ls - 2) K[s * Ls + s + 1] = 1.0;
+        else K[(Ls - 1) * Ls] = -p.mass_minus;
+      }
+    }
+    for (int i = 0; i < Ls * Ls; ++i) {
+      const double I = (i % (Ls + 1) == 0) ? 1.0 : 0.0;
+      A[i] = dg * I + od * K[i];
+      B[i] = p.b * I + p.c * K[i];
+    }
+    invert_real(Ls, A, Ai);
+    for (int i = 0; i < Ls; ++i)
+      for (int j = 0; j < Ls; ++j) {
+        double s = 0;
+        for (int k = 0; k < Ls; ++k) s += B[i * Ls + k] * Ai[k * Ls + j];
+        G[i * Ls + j] = s;
+      }
+    auto put = [&](int sl, const std::vector<double>& M, bool tr) {
+      double* d = slot(sl, ch);
+      for (int i = 0; i < Ls; ++i)
+        for (int j = 0; j < Ls; ++j) d[i * Ls + j] = tr ? M[j * Ls + i] : M[i * Ls + j];
+    };
+    put(S_A, A, false); put(S_ADAG, A, true);
+    put(S_AINV, Ai, false); put(S_AINVDAG, Ai, true);
+    put(S_B, B, false); put(S_BDAG, B, true);
+    put(S_G, G, false); put(S_GDAG, G, true);
+  }
+  op->smat_host = all;
+  if (!op->smat) op->smat = dmalloc(all.size() * op->rb());
+  if (op->prec == P64) {
+    CK(cudaMemcpy(op->smat, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> f(all.begin(), all.end());
+    CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+  }
+}
+
+void ensure_ws(gbf_op* op) {
+  if (op->ws) return;
+  const size_t h = op->half();
+  const int ntmp = 12;
+  op->ws = dmalloc(h * ntmp);
+  for (int i = 0; i < ntmp; ++i) op->tmp[i] = (char*)op->ws + (size_t)i * h;
+  const long long maxblocks = op->g.Vh + 1;
+  op->partial = (double2*)dmalloc((size_t)maxblocks * op->g.nrhs * sizeof(double2));
+  op->counter = (unsigned*)dmalloc(sizeof(unsigned) * 4);
+  CK(cudaMemset(op->counter, 0, sizeof(unsigned) * 4));
+  op->st = (CGState*)dmalloc(sizeof(CGState));
+  CK(cudaMemset(op->st, 0, sizeof(CGState)));
+  CK(cudaMallocHost(&op->hst, 2 * sizeof(CGState)));
+  CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&op->ev_in, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&op->ev_out, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&op->ev_chk[0], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&op->ev_chk[1], cudaEventDisableTiming));
+}
+
+void free_op(gbf_op* op) {
+  if (op->graph) cudaGraphExecDestroy(op->graph);
+  cudaFree(op->links);
+  cudaFree(op->clov_mem);
+  cudaFree(op->smat);
+  cudaFree(op->ws);
+  cudaFree(op->partial);
+  cudaFree(op->counter);
+  cudaFree(op->st);
+  cudaFree(op->errbits);
+  if (op->hst) cudaFreeHost(op->hst);
+  if (op->stream) cudaStreamDestroy(op->stream);
+  for (cudaEvent_t e : {op->ev_in, op->ev_out, op->ev_chk[0], op->ev_chk[1]})
+    if (e) cudaEventDestroy(e);
+  delete op;
+}
+
+// read one reduction result (all rhs) into host memory; synchronises s
+void read_last(gbf_op* op, cudaStream_t s, double* re, double* im) {
+  CK(cudaMemcpyAsync(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int r = 0; r < op->g.nrhs; ++r) {
+    if (re) re[r] = op->hst->last[r];
+    if (im) im[r] = op->hst->last_im[r];
+  }
+}
+
+const Geo& geo_for(gbf_op* op, int nhalves_4d) { return nhalves_4d ? op->g4 : op->g; }
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* gbf_last_error(void) { return g_err.c_str(); }
+
+unsigned long long gbf_launch_count(void) { return g_launches.load(); }
+
+int gbf_link_bytes(const gbf_op* op) {
+  if (!op) return 0;
+  return op->LS == L64 ? 144 : (op->LS == L32 ? 72 : 48);
+}
+
+int gbf_stream_sync(void* stream) {
+  return guarded([&] { CK(cudaStreamSynchronize((cudaStream_t)stream)); });
+}
+
+int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op** out) {
+  return guarded([&] {
+    if (!name || !params || !out) throw Fail(GBF_E_ARG, "null argument");
+    *out = nullptr;
+    std::string nm(name);
+    if (nm != "wilson_clover" && nm != "mobius") throw Fail(GBF_E_UNSUPPORTED, "unknown fermion operator " + nm);
+    if (precision < GBF_DOUBLE || precision > GBF_HALF) throw Fail(GBF_E_ARG, "bad precision");
+    const gbf_params& p = *params;
+    for (int m = 0; m < 4; ++m)
+      if (p.dims[m] < 2 || p.dims[m] % 2) throw Fail(GBF_E_ARG, "lattice dimensions must be even and >= 2");
+    if (p.n_rhs < 1 || p.n_rhs > kMaxRhs) throw Fail(GBF_E_ARG, "n_rhs must be in [1, 16]");
+    const bool mob = nm == "mobius";
+    if (mob && (p.Ls < 1 || p.Ls > kMaxLs)) throw Fail(GBF_E_ARG, "Ls must be in [1, 32]");
+    const int N5 = (mob ? p.Ls : 1) * p.n_rhs;
+    if (N5 > 256) throw Fail(GBF_E_ARG, "Ls * n_rhs must be <= 256");
+    long long V = (long long)p.dims[0] * p.dims[1] * p.dims[2] * p.dims[3];
+    if (V / 2 * N5 > (1LL << 31) / 12) throw Fail(GBF_E_ARG, "field too large for 32-bit component indexing");
+    auto* op = new gbf_op;
+    op->name = nm;
+    op->mobius = mob;
+    op->par = p;
+    op->prec = precision == GBF_DOUBLE ? P64 : (precision == GBF_SINGLE ? P32 : P16);
+    if (mob) {
+      for (int m = 0; m < 4; ++m) op->cc[m] = 1.0;
+      op->diag = 4.0 - p.M5;
+    } else {
+      const double xi0 = p.xi_0 != 0.0 ? p.xi_0 : 1.0;
+      const double nu = p.nu != 0.0 ? p.nu : 1.0;
+      for (int m = 0; m < 3; ++m) op->cc[m] = nu / xi0;
+      op->cc[3] = 1.0;
+      op->diag = p.mass + 1.0 + 3.0 * nu / xi0;
+      op->has_clover = (p.csw_r != 0.0 || p.csw_t != 0.0);
+    }
+    setup_geo(op);
+    try {
+      if (mob) build_smat(op);
+      op->errbits = (unsigned*)dmalloc(sizeof(unsigned) * 2);
+    } catch (...) {
+      free_op(op);
+      throw;
+    }
+    *out = op;
+  });
+}
+
+int gbf_delete(gbf_op* op) {
+  return guarded([&] {
+    if (op) free_op(op);
+  });
+}
+
+int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus) {
+  return guarded([&] {
+    if (!op) throw Fail(GBF_E_ARG, "null operator");
+    if (!op->mobius) throw Fail(GBF_E_UNSUPPORTED, "set_mass of wilson_clover: rebuild with gbf_update_gauge");
+    op->par.mass_plus = mass_plus;
+    op->par.mass_minus = mass_minus;
+    build_smat(op);
+    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+  });
+}
+
+int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream) {
+  return guarded([&] {
+    if (!op || !U) throw Fail(GBF_E_ARG, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    const Geo& g = op->g;
+    const size_t ubytes = (size_t)8 * g.Vh * 9 * sizeof(double2);
+    const double2* Ud = (const double2*)U;
+    void* tmpU = nullptr;
+    if (!on_device) {
+      tmpU = dmalloc(ubytes);
+      CK(cudaMemcpyAsync(tmpU, U, ubytes, cudaMemcpyHostToDevice, s));
+      Ud = (const double2*)tmpU;
+    }
+    double lam[4], ph[8];
+    for (int m = 0; m < 4; ++m) lam[m] = -0.5 * op->cc[m];
+    for (int k = 0; k < 8; ++k) ph[k] = op->par.boundary_phases[k];
+    if (!op->links) op->links = dmalloc((size_t)8 * link_bytes_per_parity_mu(op->prec == P64 ? L64 : L32, g.Vh));
+    int LS = op->prec == P64 ? L64 : L32;
+    if (op->prec != P64 && op->par.reconstruct != 0) {
+      CK(cudaMemsetAsync(op->errbits, 0, sizeof(unsigned), s));
+      CK(launch_pack_links(L32R, g, Ud, op->links, lam, ph, op->errbits, s));
+      unsigned eb = 0;
+      CK(cudaMemcpyAsync(&eb, op->errbits, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      float err;
+      std::memcpy(&err, &eb, sizeof(float));
+      if (err < 1e-6f) LS = L32R;
+      else if (op->par.reconstruct == 1) throw Fail(GBF_E_ARG, "links are not SU(3) to 1e-6: 12-real storage impossible");
+    }
+    if (LS != L32R) CK(launch_pack_links(LS, g, Ud, op->links, lam, ph, op->errbits, s));
+    op->LS = LS;
+    if (op->has_clover) {
+      const size_t c64 = (size_t)2 * 36 * g.Vh * sizeof(double2);  // one of clover / inverse, both parities
+      const size_t c32 = (size_t)2 * 18 * g.Vh * sizeof(float4);
+      const size_t mine = op->prec == P64 ? c64 : c32;
+      if (!op->clov_mem) op->clov_mem = dmalloc(2 * mine);
+      void* other = dmalloc(2 * (op->prec == P64 ? c32 : c64));
+      void *C64, *CI64, *C32, *CI32;
+      if (op->prec == P64) { C64 = op->clov_mem; CI64 = (char*)op->clov_mem + c64; C32 = other; CI32 = (char*)other + c32; }
+      else { C32 = op->clov_mem; CI32 = (char*)op->clov_mem + c32; C64 = other; CI64 = (char*)other + c64; }
+      CK(cudaMemsetAsync(op->errbits + 1, 0, sizeof(unsigned), s));
+      const double xi0 = op->par.xi_0 != 0.0 ? op->par.xi_0 : 1.0;
+      CK(launch_clover(g, Ud, op->diag, op->par.csw_r / xi0, op->par.csw_t, C64, CI64, C32, CI32, op->errbits + 1, s));
+      unsigned eb = 0;
+      CK(cudaMemcpyAsync(&eb, op->errbits + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      cudaFree(other);
+      if (eb != 0) throw Fail(GBF_E_ARG, "singular clover block");
+      const size_t perpar = mine / 2;
+      op->clov[0] = op->clov_mem;
+      op->clov[1] = (char*)op->clov_mem + perpar;
+      op->clov_inv[0] = (char*)op->clov_mem + mine;
+      op->clov_inv[1] = (char*)op->clov_mem + mine + perpar;
+    }
+    if (tmpU) {
+      CK(cudaStreamSynchronize(s));
+      cudaFree(tmpU);
+    }
+    op->gauge_set = true;
+    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+  });
+}
+
+int gbf_field_bytes(const gbf_op* op, int which, size_t* bytes) {
+  return guarded([&] {
+    if (!op || !bytes) throw Fail(GBF_E_ARG, "null argument");
+    if (which == 0) *bytes = op->half();
+    else if (which == 1) *bytes = 2 * op->half();
+    else if (which == 2) *bytes = 2 * op->half4();
+    else throw Fail(GBF_E_ARG, "bad field kind");
+  });
+}
+
+int gbf_field_import(gbf_op* op, const void* natural, void* full, int rhs, int five_d, void* stream) {
+  return guarded([&] {
+    if (!op || !natural || !full) throw Fail(GBF_E_ARG, "null argument");
+    if (rhs < 0 || rhs >= op->g.nrhs) throw Fail(GBF_E_ARG, "rhs out of range");
+    const Geo& g = (op->mobius && !five_d) ? op->g4 : op->g;
+    CK(launch_import(op->prec, g, (const double2*)natural, full, rhs, 0, (cudaStream_t)stream));
+    count_launch();
+  });
+}
+
+int gbf_field_export(gbf_op* op, const void* full, void* natural, int rhs, int five_d, void* stream) {
+  return guarded([&] {
+    if (!op || !natural || !full) throw Fail(GBF_E_ARG, "null argument");
+    if (rhs < 0 || rhs >= op->g.nrhs) throw Fail(GBF_E_ARG, "rhs out of range");
+    const Geo& g = (op->mobius && !five_d) ? op->g4 : op->g;
+    CK(launch_import(op->prec, g, (const double2*)natural, const_cast<void*>(full), rhs, 1, (cudaStream_t)stream));
+    count_launch();
+  });
+}
+
+int gbf_norm2(gbf_op* op, const void* x, int nhalves, double* out, void* stream) {
+  double im[kMaxRhs];
+  return gbf_inner(op, x, x, nhalves, out, im, stream);
+}
+
+int gbf_inner(gbf_op* op, const void* x, const void* y, int nhalves, double* out_re, double* out_im, void* stream) {
+  return guarded([&] {
+    if (!op || !x || !y) throw Fail(GBF_E_ARG, "null argument");
+    if (nhalves != 1 && nhalves != 2) throw Fail(GBF_E_ARG, "nhalves must be 1 or 2");
+    ensure_ws(op);
+    cudaStream_t s = (cudaStream_t)stream;
+    double re[kMaxRhs] = {0}, imv[kMaxRhs] = {0};
+    for (int h = 0; h < nhalves; ++h) {
+      BlasArgs a{};
+      a.g = op->g;
+      a.x = (const char*)x + h * op->half();
+      a.y = (const char*)y + h * op->half();
+      a.red = 3;
+      a.ra = op->red(FIN_STORE);
+      CK(launch_blas(op->prec, a, s));
+      count_launch();
+      double r1[kMaxRhs], i1[kMaxRhs];
+      read_last(op, s, r1, i1);
+      for (int r = 0; r < op->g.nrhs; ++r) { re[r] += r1[r]; imv[r] += i1[r]; }
+    }
+    for (int r = 0; r < op->g.nrhs; ++r) {
+      if (out_re) out_re[r] = re[r];
+      if (out_im) out_im[r] = imv[r];
+    }
+  });
+}
+
+int gbf_axpby(gbf_op* op, void* out, const double* a_re, const double* a_im, const void* x, const double* b, const void* y,
+              int nhalves, void* stream) {
+  return guarded([&] {
+    if (!op || !out || !x || !a_re) throw Fail(GBF_E_ARG, "null argument");
+    ensure_ws(op);
+    for (int h = 0; h < nhalves; ++h) {
+      BlasArgs a{};
+      a.g = op->g;
+      a.out = (char*)out + h * op->half();
+      a.x = (const char*)x + h * op->half();
+      a.y = y ? (const char*)y + h * op->half() : nullptr;
+      for (int r = 0; r < op->g.nrhs; ++r) {
+        a.a_re[r] = a_re[r];
+        a.a_im[r] = a_im ? a_im[r] : 0.0;
+        a.b_re[r] = b ? b[r] : 0.0;
+      }
+      a.write = 1;
+      a.red = 0;
+      a.ra = op->red(FIN_STORE);
+      CK(launch_blas(op->prec, a, (cudaStream_t)stream));
+      count_launch();
+    }
+  });
+}
+
+int gbf_convert(gbf_op* dst_op, void* dst, gbf_op* src_op, const void* src, double scale, int nhalves, void* stream) {
+  return guarded([&] {
+    if (!dst_op || !src_op || !dst || !src) throw Fail(GBF_E_ARG, "null argument");
+    if (dst_op->g.N != src_op->g.N) throw Fail(GBF_E_ARG, "operators have different field geometry");
+    for (int h = 0; h < nhalves; ++h)
+      CK(launch_convert(dst_op->prec, (char*)dst + h * dst_op->half(), src_op->prec, (const char*)src + h * src_op->half(),
+                        dst_op->g.N, scale, (cudaStream_t)stream));
+    count_launch(nhalves);
+  });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// opcode dispatch (lib/cgpt/lib/operators/unary.h:20-48 analogue)
+// ---------------------------------------------------------------------------
+static void apply_one(gbf_op* op, int opcode, const void* src, void* dst, int sp, cudaStream_t s) {
+  const size_t h = op->half();
+  auto H = [&](const void* f, int p) { return (const void*)((const char*)f + p * h); };
+  auto HW = [&](void* f, int p) { return (void*)((char*)f + p * h); };
+  const bool mob = op->mobius;
+  switch (opcode) {
+    case GBF_MEOOE:
+    case GBF_MEOOE_DAG:
+    case GBF_DHOP_EO:
+    case GBF_DHOP_EO_DAG: {
+      if (sp != GBF_EVEN && sp != GBF_ODD) throw Fail(GBF_E_ARG, "even-odd opcode needs src_parity 0 or 1");
+      const bool dag = opcode == GBF_MEOOE_DAG || opcode == GBF_DHOP_EO_DAG;
+      const bool meo = opcode == GBF_MEOOE || opcode == GBF_MEOOE_DAG;
+      if (mob && meo && !dag) {
+        op->local(s, sp, src, op->tmp[0], op->B(false));
+        op->dslash(s, 1 - sp, false, op->tmp[0], dst, op->none());
+      } else {
+        op->dslash(s, 1 - sp, dag, src, dst, (mob && meo) ? op->B(true) : op->none());
+      }
+      break;
+    }
+    case GBF_MOOEE:
+    case GBF_MOOEE_DAG:
+      op->local(s, sp, src, dst, op->A(opcode == GBF_MOOEE_DAG));
+      break;
+    case GBF_MOOEE_INV:
+    case GBF_MOOEE_INV_DAG:
+      op->local(s, sp, src, dst, op->Ainv(opcode == GBF_MOOEE_INV_DAG));
+      break;
+    case GBF_MDIAG:
+      for (int p = 0; p < 2; ++p) op->local(s, p, H(src, p), HW(dst, p), op->A(false));
+      break;
+    case GBF_DHOP:
+    case GBF_DHOP_DAG:
+      for (int p = 0; p < 2; ++p) op->dslash(s, p, opcode == GBF_DHOP_DAG, H(src, 1 - p), HW(dst, p), op->none());
+      break;
+    case GBF_M:
+    case GBF_MDAG: {
+      const bool dag = opcode == GBF_MDAG;
+      for (int p = 0; p < 2; ++p) {
+        if (!mob) {
+          op->dslash(s, p, dag, H(src, 1 - p), HW(dst, p), op->none(), 1.0, H(src, p), 1.0, op->A(dag));
+        } else {
+          op->local(s, p, H(src, p), op->tmp[1], op->A(dag));
+          if (!dag) {
+            op->local(s, 1 - p, H(src, 1 - p), op->tmp[0], op->B(false));
+            op->dslash(s, p, false, op->tmp[0], HW(dst, p), op->none(), 1.0, op->tmp[1], 1.0);
+          } else {
+            op->dslash(s, p, true, H(src, 1 - p), HW(dst, p), op->B(true), 1.0, op->tmp[1], 1.0);
+          }
+        }
+      }
+      break;
+    }
+    case GBF_DMINUS:
+    case GBF_DMINUS_DAG: {
+      if (!mob) {  // Wilson: Dminus is the identity (reference/wilson_clover.py:174-176)
+        CK(cudaMemcpyAsync(dst, src, 2 * h, cudaMemcpyDeviceToDevice, s));
+        break;
+      }
+      // psi - c D_W psi, D_W = (4 - M5) + Dhop, slice by slice
+      const double c = op->par.c, d = 1.0 - c * (4.0 - op->par.M5);
+      for (int p = 0; p < 2; ++p)
+        op->dslash(s, p, opcode == GBF_DMINUS_DAG, H(src, 1 - p), HW(dst, p), op->none(), -c, H(src, p), d);
+      break;
+    }
+    default:
+      throw Fail(GBF_E_UNSUPPORTED, "opcode " + std::to_string(opcode) + " not supported");
+  }
+}
+
+// Mobius wall transfer (4D <-> 5D) on one parity of internal fields.
+template <int P>
+__global__ void wall_kernel(Geo g, Geo g4, const void* in, void* out, int to5d) {
+  using R = typename SpinorT<P>::R;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g4.N) return;  // one thread per (4D site, rhs)
+  const long long cb = t / g4.N5;
+  const int rhs = (int)(t - cb * g4.N5);
+  const long long n0 = cb * g.N5 + (long long)rhs * g.Ls, nl = n0 + g.Ls - 1;
+  cplx<R> v[12], w[12];
+  if (to5d) {
+    // s = 0 gets P+ eta, s = Ls-1 gets P- eta (the convention that reproduces
+    // the reference's ImportPhysicalFermionSource fingerprint)
+    load_spinor<P>(in, g4.N, t, v);
+    for (int k = 0; k < 12; ++k) w[k] = (k < 6) ? v[k] : cz<R>();
+    store_spinor<P>(out, g.N, n0, w);
+    for (int k = 0; k < 12; ++k) w[k] = (k < 6) ? cz<R>() : v[k];
+    store_spinor<P>(out, g.N, nl, w);
+  } else {
+    // q = P- psi_0 + P+ psi_{Ls-1}  (lib/gpt/qcd/fermion/mobius.py:162)
+    load_spinor<P>(in, g.N, n0, v);
+    load_spinor<P>(in, g.N, nl, w);
+    for (int k = 0; k < 6; ++k) v[k] = w[k];
+    store_spinor<P>(out, g4.N, t, v);
+  }
+}
+
+static void wall(gbf_op* op, const void* in, void* out, int to5d, cudaStream_t s) {
+  const unsigned nb = (unsigned)((op->g4.N + 255) / 256);
+  for (int p = 0; p < 2; ++p) {
+    const void* i = (const char*)in + p * (to5d ? op->half4() : op->half());
+    void* o = (char*)out + p * (to5d ? op->half() : op->half4());
+    if (op->prec == P64) wall_kernel<P64><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
+    else if (op->prec == P32) wall_kernel<P32><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
+    else wall_kernel<P16><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
+    CK(cudaGetLastError());
+    count_launch();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// eo2_ne CG iteration.  D = odd sites (the reference default parity), C = even.
+//   G = C_C^-1 / C_D^-1 (Wilson-clover) or B A^-1 (Mobius), so that
+//   Mpc = 1 - Dhop G Dhop G and Mpc^+ = 1 - G^+ Dhop^+ G^+ Dhop^+.
+// Workspace: tmp[0..1] t, z ; tmp[2..3] w, u ; tmp[4] p ; tmp[5] r ; tmp[6] mmp ;
+//            tmp[7] y (CG solution) ; tmp[8..9] prepare/reconstruct scratch.
+// ---------------------------------------------------------------------------
+static constexpr int kKernelsPerIteration = 6;
+
+// ev (optional, profile mode): 7 events recorded around the six launches
+static void cg_iteration(gbf_op* op, cudaStream_t s, cudaEvent_t* ev = nullptr) {
+  const int D = GBF_ODD, C = GBF_EVEN;
+  void *t = op->tmp[0], *z = op->tmp[1], *w = op->tmp[2], *u = op->tmp[3];
+  void *p = op->tmp[4], *r = op->tmp[5], *mmp = op->tmp[6], *y = op->tmp[7];
+  auto mark = [&](int i) {
+    if (ev) CK(cudaEventRecord(ev[i], s));
+  };
+  mark(0);
+  // p = r + beta p ; t = G_D p
+  op->local(s, D, r, t, op->G(), 1.0, nullptr, 0.0, p, 1, 0, nullptr, FIN_STORE, 1);
+  mark(1);
+  // z = G_C Dhop t
+  op->dslash(s, C, false, t, z, op->G(), 1.0, nullptr, 0.0, op->none(), 0, nullptr, FIN_STORE, 1);
+  mark(2);
+  // w = p - Dhop z
+  op->dslash(s, D, false, z, w, op->none(), -1.0, p, 1.0, op->none(), 0, nullptr, FIN_STORE, 1);
+  mark(3);
+  // u = G_C^+ Dhop^+ w
+  op->dslash(s, C, true, w, u, op->Gdag(), 1.0, nullptr, 0.0, op->none(), 0, nullptr, FIN_STORE, 1);
+  mark(4);
+  // mmp = w - G_D^+ Dhop^+ u ; d = Re <p, mmp> -> alpha
+  op->dslash(s, D, true, u, mmp, op->Gdag(), -1.0, w, 1.0, op->none(), 1, p, FIN_ALPHA, 1);
+  mark(5);
+  // r -= alpha mmp ; y += alpha p ; |r|^2 -> beta, convergence
+  op->cg_update(s, r, mmp, y, p);
+  mark(6);
+}
+
+extern "C" {
+
+int gbf_apply(gbf_op* op, int opcode, const void* const* src, void* const* dst, int n, int src_parity, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !dst || n < 0) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    ensure_ws(op);
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int i = 0; i < n; ++i) {
+      if (!src[i] || !dst[i]) throw Fail(GBF_E_ARG, "null field");
+      if (src[i] == dst[i]) throw Fail(GBF_E_ARG, "src and dst must differ (as in the reference)");
+      if (opcode == GBF_IMPORT_PHYSICAL_FERMION_SOURCE || opcode == GBF_EXPORT_PHYSICAL_FERMION_SOLUTION) {
+        if (!op->mobius) {
+          CK(cudaMemcpyAsync(dst[i], src[i], 2 * op->half(), cudaMemcpyDeviceToDevice, s));
+        } else if (opcode == GBF_IMPORT_PHYSICAL_FERMION_SOURCE) {
+          // walls, then Dminus
+          void* t = op->tmp[2];  // tmp[2], tmp[3] form one contiguous full field
+          CK(cudaMemsetAsync(t, 0, 2 * op->half(), s));
+          wall(op, src[i], t, 1, s);
+          apply_one(op, GBF_DMINUS, t, dst[i], GBF_FULL, s);
+        } else {
+          wall(op, src[i], dst[i], 0, s);
+        }
+        continue;
+      }
+      apply_one(op, opcode, src[i], dst[i], src_parity, s);
+    }
+  });
+}
+
+int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* prm, gbf_cg_result* res, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !x || !prm) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    ensure_ws(op);
+    cudaStream_t user = (cudaStream_t)stream;
+    cudaStream_t s = op->stream;
+    CK(cudaEventRecord(op->ev_in, user));
+    CK(cudaStreamWaitEvent(s, op->ev_in, 0));
+    const int D = GBF_ODD, C = GBF_EVEN;
+    const size_t h = op->half();
+    const void* srcC = (const char*)src + C * h;
+    const void* srcD = (const char*)src + D * h;
+    void* xC = (char*)x + C * h;
+    void* xD = (char*)x + D * h;
+    void *p = op->tmp[4], *r = op->tmp[5], *y = op->tmp[7], *s1 = op->tmp[8], *tC = op->tmp[9], *u = op->tmp[3];
+    // ---- prepare: r = Mpc^+ (src_D - Dhop G_C src_C)  (R_ne, normal_equation.py:47-48) ----
+    op->local(s, C, srcC, tC, op->G());
+    op->dslash(s, D, false, tC, s1, op->none(), -1.0, srcD, 1.0);
+    op->dslash(s, C, true, s1, u, op->Gdag());
+    op->dslash(s, D, true, u, r, op->Gdag(), -1.0, s1, 1.0, op->none(), 2, nullptr, FIN_STORE);
+    CK(launch_cg_init(op->st, op->g.nrhs, prm->eps, prm->maxiter, s));
+    count_launch();
+    CK(cudaMemsetAsync(p, 0, h, s));
+    CK(cudaMemsetAsync(y, 0, h, s));
+    double kms[3] = {0, 0, 0};
+    int kcount[3] = {0, 0, 0};
+    if (prm->profile) {
+      // diagnostic: plain launches with CUDA events around each kernel class
+      cudaEvent_t ev[7];
+      for (int i = 0; i < 7; ++i) CK(cudaEventCreate(&ev[i]));
+      for (int it = 0; it < prm->maxiter; ++it) {
+        cg_iteration(op, s, ev);
+        CK(cudaEventSynchronize(ev[6]));
+        float ms;
+        CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        kms[1] += ms;
+        for (int i = 1; i < 5; ++i) {
+          CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+          kms[0] += ms;
+        }
+        CK(cudaEventElapsedTime(&ms, ev[5], ev[6]));
+        kms[2] += ms;
+        kcount[0] += 4;
+        kcount[1] += 1;
+        kcount[2] += 1;
+        CK(cudaMemcpy(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost));
+        if (op->hst->all_done) break;
+      }
+      for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+    }
+    // ---- CG loop in graphs of K iterations ----
+    const int K = prm->iterations_per_graph > 0 ? prm->iterations_per_graph : 8;
+    if (!prm->profile && (!op->graph || op->graph_K != K)) {
+      if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+      cudaGraph_t gr;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int k = 0; k < K; ++k) cg_iteration(op, s);
+      } catch (...) {
+        cudaStreamEndCapture(s, &gr);
+        throw;
+      }
+      CK(cudaStreamEndCapture(s, &gr));
+      CK(cudaGraphInstantiate(&op->graph, gr, 0));
+      cudaGraphDestroy(gr);
+      op->graph_K = K;
+    }
+    const int max_launches = prm->profile ? 0 : (prm->maxiter + K - 1) / K;
+    bool done = false;
+    int launched = 0;
+    for (; launched < max_launches && !done; ++launched) {
+      CK(cudaGraphLaunch(op->graph, s));
+      count_launch((unsigned long long)K * kKernelsPerIteration);
+      CK(cudaMemcpyAsync(op->hst + (launched & 1), op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+      CK(cudaEventRecord(op->ev_chk[launched & 1], s));
+      if (launched > 0) {
+        CK(cudaEventSynchronize(op->ev_chk[(launched - 1) & 1]));
+        done = op->hst[(launched - 1) & 1].all_done != 0;
+      }
+    }
+    CK(cudaStreamSynchronize(s));
+    // ---- reconstruct: x_D = A^-1 y ; x_C = A_C^-1 (src_C - Dhop G y) ----
+    op->local(s, D, y, xD, op->Ainv(false));
+    op->local(s, D, y, tC, op->G());
+    op->dslash(s, C, false, tC, s1, op->none(), -1.0, srcC, 1.0);
+    op->local(s, C, s1, xC, op->Ainv(false));
+    CK(cudaMemcpyAsync(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(op->ev_out, s));
+    CK(cudaStreamWaitEvent(user, op->ev_out, 0));
+    CK(cudaEventSynchronize(op->ev_out));
+    const CGState& st = op->hst[0];
+    if (res) {
+      res->iterations = st.iter;
+      int conv = 1;
+      for (int k = 0; k < op->g.nrhs; ++k) {
+        const double b2 = st.last[k];  // |b|^2 of the eo2_ne system from the prepare reduction
+        res->residual_sq[k] = b2 > 0 ? st.cp[k] / b2 : 0.0;
+        conv &= (st.cp[k] <= st.rsq[k]) ? 1 : 0;
+      }
+      res->converged = conv;
+      res->breakdown = st.breakdown;
+      for (int i = 0; i < 3; ++i) {
+        res->kernel_ms[i] = kms[i];
+        res->kernel_launches[i] = kcount[i];
+      }
+    }
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,249 @@
+// gbf_common.cuh -- shared device types for the GB300 fermion-matrix kernels.
+//
+// Internal field layout (one checkerboard half):
+//   a "5D site" n = cb4 * N5 + i5, with cb4 the checkerboard index of the 4D
+//   site and i5 = rhs * Ls + s the inner index (Ls = 1 for Wilson-clover).
+//   Consecutive threads take consecutive n, so every component load is a
+//   fully coalesced 16-byte vector load:
+//     FP64: double2 [12][N]             (192 B per 5D site)
+//     FP32: float4  [6][N]              ( 96 B per 5D site)
+//     FP16: uint4   [3][N] + float [N]  ( 52 B per 5D site; __half2 values
+//           normalised by a per-site FP32 scale = max |component|)
+//   A full field is [even half][odd half].
+//   cb4 = (x0/2) + (L0/2)*(x1 + L1*(x2 + L2*x3)); parity = (x0+x1+x2+x3) & 1.
+//
+// Gauge links, [parity][mu][chunk][Vh] for the sites of that parity:
+//     L64  : double2 [9]  (full 3x3, boundary phase and -cc_mu/2 folded in)
+//     L32  : float2  [9]  (same, FP32)
+//     L32R : float4  [3]  (rows 0,1 of an SU(3) matrix; row 2 rebuilt as
+//                          conj(row0 x row1); phase and -cc_mu/2 at run time)
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cstdint>
+
+namespace gbf {
+
+enum Prec { P64 = 0, P32 = 1, P16 = 2 };
+enum LinkStore { L64 = 0, L32 = 1, L32R = 2 };
+enum LocalKind { LOC_NONE = 0, LOC_CLOVER = 1, LOC_SMAT = 2, LOC_SCALAR = 3 };
+
+constexpr int kMaxLs = 32;
+constexpr int kMaxRhs = 16;
+
+// Geometry and run-time constants of one operator.
+struct Geo {
+  int L[4];
+  int Lh0;      // L0 / 2
+  int Vh;       // 4D sites per parity
+  int N5;       // inner extent = Ls * nrhs
+  int Ls;       // 5th dimension (1 for Wilson-clover)
+  int nrhs;
+  long long N;  // 5D sites per parity = Vh * N5
+  // run-time link factors for reconstructed links: lambda_mu = -cc_mu/2 and phase_mu
+  float lam[4];
+  float ph_re[4], ph_im[4];
+};
+
+template <typename R> struct C2;
+template <> struct C2<double> { using T = double2; };
+template <> struct C2<float> { using T = float2; };
+template <typename R> using cplx = typename C2<R>::T;
+
+template <typename R> __device__ __forceinline__ cplx<R> mk(R a, R b) { cplx<R> r; r.x = a; r.y = b; return r; }
+template <typename R> __device__ __forceinline__ cplx<R> cz() { return mk<R>(0, 0); }
+template <typename R> __device__ __forceinline__ cplx<R> add(cplx<R> a, cplx<R> b) { return mk<R>(a.x + b.x, a.y + b.y); }
+template <typename R> __device__ __forceinline__ cplx<R> sub(cplx<R> a, cplx<R> b) { return mk<R>(a.x - b.x, a.y - b.y); }
+template <typename R> __device__ __forceinline__ cplx<R> scl(R s, cplx<R> a) { return mk<R>(s * a.x, s * a.y); }
+// acc + a*b
+template <typename R> __device__ __forceinline__ cplx<R> cmadd(cplx<R> acc, cplx<R> a, cplx<R> b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(a.y, b.x, acc.y);
+  return acc;
+}
+// acc + conj(a)*b
+template <typename R> __device__ __forceinline__ cplx<R> cmaddc(cplx<R> acc, cplx<R> a, cplx<R> b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(-a.y, b.x, acc.y);
+  return acc;
+}
+template <typename R> __device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) { return cmadd<R>(cz<R>(), a, b); }
+
+// ---------------------------------------------------------------------------
+// spinor storage
+// ---------------------------------------------------------------------------
+template <int P> struct SpinorT;
+template <> struct SpinorT<P64> { using R = double; static constexpr int bytes = 192; };
+template <> struct SpinorT<P32> { using R = float; static constexpr int bytes = 96; };
+template <> struct SpinorT<P16> { using R = float; static constexpr int bytes = 52; };
+
+__host__ __device__ inline long long half_bytes(int P, long long N) {
+  return P == P64 ? 192 * N : (P == P32 ? 96 * N : 52 * N);
+}
+
+template <int P> __device__ __forceinline__ void load_spinor(const void* base, long long N, long long n, cplx<typename SpinorT<P>::R> (&v)[12]);
+template <int P> __device__ __forceinline__ void store_spinor(void* base, long long N, long long n, const cplx<typename SpinorT<P>::R> (&v)[12]);
+
+template <> __device__ __forceinline__ void load_spinor<P64>(const void* base, long long N, long long n, double2 (&v)[12]) {
+  const double2* p = reinterpret_cast<const double2*>(base) + n;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) v[k] = __ldg(p + k * N);
+}
+template <> __device__ __forceinline__ void store_spinor<P64>(void* base, long long N, long long n, const double2 (&v)[12]) {
+  double2* p = reinterpret_cast<double2*>(base) + n;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) p[k * N] = v[k];
+}
+template <> __device__ __forceinline__ void load_spinor<P32>(const void* base, long long N, long long n, float2 (&v)[12]) {
+  const float4* p = reinterpret_cast<const float4*>(base) + n;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    float4 q = __ldg(p + k * N);
+    v[2 * k] = make_float2(q.x, q.y);
+    v[2 * k + 1] = make_float2(q.z, q.w);
+  }
+}
+template <> __device__ __forceinline__ void store_spinor<P32>(void* base, long long N, long long n, const float2 (&v)[12]) {
+  float4* p = reinterpret_cast<float4*>(base) + n;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) p[k * N] = make_float4(v[2 * k].x, v[2 * k].y, v[2 * k + 1].x, v[2 * k + 1].y);
+}
+template <> __device__ __forceinline__ void load_spinor<P16>(const void* base, long long N, long long n, float2 (&v)[12]) {
+  const uint4* p = reinterpret_cast<const uint4*>(base) + n;
+  const float s = __ldg(reinterpret_cast<const float*>(reinterpret_cast<const uint4*>(base) + 3 * N) + n);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    uint4 q = __ldg(p + k * N);
+    const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      __half2 h = *reinterpret_cast<const __half2*>(&w[j]);
+      float2 f = __half22float2(h);
+      v[4 * k + j] = make_float2(f.x * s, f.y * s);
+    }
+  }
+}
+template <> __device__ __forceinline__ void store_spinor<P16>(void* base, long long N, long long n, const float2 (&v)[12]) {
+  float m = 0.f;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
+  const float inv = m > 0.f ? 1.f / m : 0.f;
+  uint4* p = reinterpret_cast<uint4*>(base) + n;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    unsigned w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      __half2 h = __floats2half2_rn(v[4 * k + j].x * inv, v[4 * k + j].y * inv);
+      w[j] = *reinterpret_cast<unsigned*>(&h);
+    }
+    p[k * N] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  reinterpret_cast<float*>(reinterpret_cast<uint4*>(base) + 3 * N)[n] = m;
+}
+
+// ---------------------------------------------------------------------------
+// links
+// ---------------------------------------------------------------------------
+template <int LS> struct LinkT;
+template <> struct LinkT<L64> { using R = double; static constexpr int chunks = 9; static constexpr int chunk_bytes = 16; };
+template <> struct LinkT<L32> { using R = float; static constexpr int chunks = 9; static constexpr int chunk_bytes = 8; };
+template <> struct LinkT<L32R> { using R = float; static constexpr int chunks = 3; static constexpr int chunk_bytes = 16; };
+
+__host__ __device__ inline long long link_bytes_per_parity_mu(int LS, int Vh) {
+  return (long long)Vh * (LS == L64 ? 144 : (LS == L32 ? 72 : 48));
+}
+
+// Load U_mu at checkerboard index cb of parity p into u[9] (row major).
+template <int LS, typename R>
+__device__ __forceinline__ void load_link(const void* links, int Vh, int p, int mu, int cb, cplx<R> (&u)[9]);
+
+template <> __device__ __forceinline__ void load_link<L64, double>(const void* links, int Vh, int p, int mu, int cb, double2 (&u)[9]) {
+  const double2* b = reinterpret_cast<const double2*>(links) + (size_t)(p * 4 + mu) * 9 * Vh + cb;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (size_t)k * Vh);
+}
+template <> __device__ __forceinline__ void load_link<L32, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
+  const float2* b = reinterpret_cast<const float2*>(links) + (size_t)(p * 4 + mu) * 9 * Vh + cb;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (size_t)k * Vh);
+}
+template <> __device__ __forceinline__ void load_link<L32R, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
+  const float4* b = reinterpret_cast<const float4*>(links) + (size_t)(p * 4 + mu) * 3 * Vh + cb;
+  float4 a0 = __ldg(b), a1 = __ldg(b + Vh), a2 = __ldg(b + 2 * (size_t)Vh);
+  u[0] = make_float2(a0.x, a0.y); u[1] = make_float2(a0.z, a0.w); u[2] = make_float2(a1.x, a1.y);
+  u[3] = make_float2(a1.z, a1.w); u[4] = make_float2(a2.x, a2.y); u[5] = make_float2(a2.z, a2.w);
+  // row2 = conj(row0 x row1)
+  u[6] = make_float2(u[1].x * u[5].x - u[1].y * u[5].y - (u[2].x * u[4].x - u[2].y * u[4].y),
+                     -(u[1].x * u[5].y + u[1].y * u[5].x - (u[2].x * u[4].y + u[2].y * u[4].x)));
+  u[7] = make_float2(u[2].x * u[3].x - u[2].y * u[3].y - (u[0].x * u[5].x - u[0].y * u[5].y),
+                     -(u[2].x * u[3].y + u[2].y * u[3].x - (u[0].x * u[5].y + u[0].y * u[5].x)));
+  u[8] = make_float2(u[0].x * u[4].x - u[0].y * u[4].y - (u[1].x * u[3].x - u[1].y * u[3].y),
+                     -(u[0].x * u[4].y + u[0].y * u[4].x - (u[1].x * u[3].y + u[1].y * u[3].x)));
+}
+
+// ---------------------------------------------------------------------------
+// gamma matrices of the gpt/Grid basis (lib/gpt/core/gamma.py:28-41):
+// gamma_mu[r][perm(mu,r)] = coef(mu,r), coef in {+1,-1,+i,-i}
+// coef codes: 0:+1 1:-1 2:+i 3:-i
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int gperm(int mu, int r) { return (mu < 2) ? (3 - r) : ((r + 2) & 3); }
+__host__ __device__ constexpr int gcoef(int mu, int r) {
+  return mu == 0 ? (r < 2 ? 2 : 3) : mu == 1 ? (r == 0 || r == 3 ? 1 : 0) : mu == 2 ? (r == 0 || r == 3 ? 2 : 3) : 0;
+}
+// s * coef * v  (s = +-1 as a real factor)
+template <typename R> __device__ __forceinline__ cplx<R> coefmul(int code, R s, cplx<R> v) {
+  switch (code) {
+    case 0: return mk<R>(s * v.x, s * v.y);
+    case 1: return mk<R>(-s * v.x, -s * v.y);
+    case 2: return mk<R>(-s * v.y, s * v.x);
+    default: return mk<R>(s * v.y, -s * v.x);
+  }
+}
+// a + s * coef * v as fused multiply-adds
+template <typename R> __device__ __forceinline__ cplx<R> coefmadd(int code, R s, cplx<R> v, cplx<R> a) {
+  switch (code) {
+    case 0: return mk<R>(fma(s, v.x, a.x), fma(s, v.y, a.y));
+    case 1: return mk<R>(fma(-s, v.x, a.x), fma(-s, v.y, a.y));
+    case 2: return mk<R>(fma(-s, v.y, a.x), fma(s, v.x, a.y));
+    default: return mk<R>(fma(s, v.y, a.x), fma(-s, v.x, a.y));
+  }
+}
+
+// 4D coordinates of checkerboard index cb at parity p
+struct Coord { int x[4]; };
+__device__ __forceinline__ Coord cb_coords(const Geo& g, int cb, int p) {
+  Coord c;
+  int xh = cb % g.Lh0;
+  int r = cb / g.Lh0;
+  c.x[1] = r % g.L[1];
+  r /= g.L[1];
+  c.x[2] = r % g.L[2];
+  c.x[3] = r / g.L[2];
+  c.x[0] = 2 * xh + ((c.x[1] + c.x[2] + c.x[3] + p) & 1);
+  return c;
+}
+__device__ __forceinline__ int cb_index(const Geo& g, const int (&x)[4]) {
+  return (x[0] >> 1) + g.Lh0 * (x[1] + g.L[1] * (x[2] + g.L[2] * x[3]));
+}
+
+// ---------------------------------------------------------------------------
+// reductions: deterministic two-level sum (fixed block order)
+// ---------------------------------------------------------------------------
+struct CGState {
+  double cp[kMaxRhs];    // |r|^2
+  double rsq[kMaxRhs];   // eps^2 |b|^2
+  double alpha[kMaxRhs];
+  double beta[kMaxRhs];
+  double d[kMaxRhs];
+  double last[kMaxRhs];  // last reduction result (generic)
+  double last_im[kMaxRhs];
+  int done[kMaxRhs];
+  int all_done;
+  int iter;
+  int nrhs;
+  int breakdown;
+  int maxiter;
+};
+
+}  // namespace gbf

@@ -1,0 +1,204 @@
+// gbf_dslash.cu -- the even-odd Wilson hopping kernel with fused epilogues.
+//
+// Computes, for every 5D site n of the output parity p (thread per site):
+//   hop(x) = -1/2 sum_mu cc_mu [ (1 + s g_mu) U_mu(x) in(x+mu)
+//                               + (1 - s g_mu) U_mu(x-mu)^+ in(x-mu) ]
+// with s = -1 for Dhop and s = +1 for Dhop^dag (the statement of
+// lib/gpt/qcd/fermion/reference/wilson_clover.py:182-200, which Grid's
+// WilsonKernels implement for opcodes 3001/3002/4001/4002, and the 4D part of
+// Grid's Cayley Meooe for Mobius), followed by the epilogue
+//   out = c1 * L1(hop) + c2 * L2(X)       (L1, L2 site-local operators)
+// and optionally the deterministic reduction of <Y, out> or |out|^2 with a
+// CG finaliser.  The input spinor is projected to two spin components before
+// the colour multiply (8 x 2 SU(3) matvecs per site) and the lower two spin
+// components of each term are rebuilt from the upper two.
+//
+// Roofline: HBM-bound in FP32/FP16 (per output site: 8 neighbour spinors that
+// the L2 mostly serves once, 8 links, 1 output); FP64 is bound by the FP64
+// pipe on GB300 (about 1.2 TFLOP/s measured).
+#include "gbf_launch.cuh"
+
+namespace gbf {
+
+
+template <int P, int LS, int LK>
+__global__ void __launch_bounds__(256) dslash_kernel(const DslashArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  extern __shared__ double smem_d[];
+  const Geo& g = a.g;
+  if (a.check_done && a.ra.st->all_done) return;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = n < g.N;
+  const int p = a.out_parity, q = 1 - p;
+  V res[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) res[k] = cz<R>();
+  int cb = 0;
+  if (active) {
+    cb = (int)(n / g.N5);
+    const int i5 = (int)(n - (long long)cb * g.N5);
+    const Coord c = cb_coords(g, cb, p);
+    const R sf = (R)a.sgn;
+#pragma unroll
+    for (int mu = 0; mu < 4; ++mu) {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir) {
+        int y[4] = {c.x[0], c.x[1], c.x[2], c.x[3]};
+        const bool fwd = dir == 0;
+        bool wrap;
+        if (fwd) {
+          wrap = (y[mu] == g.L[mu] - 1);
+          y[mu] = wrap ? 0 : y[mu] + 1;
+        } else {
+          wrap = (y[mu] == 0);
+          y[mu] = wrap ? g.L[mu] - 1 : y[mu] - 1;
+        }
+        const int ycb = cb_index(g, y);
+        V psi[12];
+        load_spinor<P>(a.in, g.N, (long long)ycb * g.N5 + i5, psi);
+        // project: h_r = psi_r + s * coef_r * psi_perm(r), r = 0, 1
+        const R s = fwd ? sf : -sf;
+        V h[2][3];
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int col = 0; col < 3; ++col)
+            h[r][col] = coefmadd<R>(gcoef(mu, r), s, psi[3 * gperm(mu, r) + col], psi[3 * r + col]);
+        V u[9];
+        load_link<LS, R>(a.links, g.Vh, fwd ? p : q, mu, fwd ? cb : ycb, u);
+        V uh[2][3];
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            V acc = cz<R>();
+#pragma unroll
+            for (int j = 0; j < 3; ++j) acc = fwd ? cmadd<R>(acc, u[3 * i + j], h[r][j]) : cmaddc<R>(acc, u[3 * j + i], h[r][j]);
+            uh[r][i] = acc;
+          }
+        if (LS == L32R) {
+          // lambda = -cc/2 times the boundary phase (conjugated for the backward link)
+          const R lam = (R)g.lam[mu];
+          V ph = mk<R>(lam, (R)0);
+          if (wrap) ph = mk<R>(lam * (R)g.ph_re[mu], (fwd ? lam : -lam) * (R)g.ph_im[mu]);
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) uh[r][i] = cmul<R>(ph, uh[r][i]);
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) res[3 * r + i] = add<R>(res[3 * r + i], uh[r][i]);
+#pragma unroll
+        for (int r = 2; r < 4; ++r)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) res[3 * r + i] = coefmadd<R>(gcoef(mu, r), s, uh[gperm(mu, r)][i], res[3 * r + i]);
+      }
+    }
+  }
+  // ---- epilogue ----
+  if (LK == LOC_SMAT) {
+    if (a.l1.kind == LOC_SMAT) {
+      R* tile = reinterpret_cast<R*>(smem_d);
+      R* mat = tile + 24 * blockDim.x;
+      smat_apply_block<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res, true);
+    }
+  } else if (active && a.l1.kind != LOC_NONE) {
+    local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
+  }
+  if (active) {
+    if (a.c1 != 1.0) {
+      const R c1 = (R)a.c1;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) res[k] = scl<R>(c1, res[k]);
+    }
+    if (a.X) {
+      V xv[12];
+      load_spinor<P>(a.X, g.N, n, xv);
+      if (LK != LOC_SMAT && a.l2.kind != LOC_NONE) local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+      const R c2 = (R)a.c2;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) res[k] = mk<R>(fma(c2, xv[k].x, res[k].x), fma(c2, xv[k].y, res[k].y));
+    }
+    store_spinor<P>(a.out, g.N, n, res);
+  }
+  if (a.red) {
+    double vr = 0, vi = 0;
+    if (active) {
+      if (a.red == 1) {
+        V yv[12];
+        load_spinor<P>(a.Y, g.N, n, yv);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+          vr += (double)yv[k].x * res[k].x + (double)yv[k].y * res[k].y;
+          vi += (double)yv[k].x * res[k].y - (double)yv[k].y * res[k].x;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) vr += (double)res[k].x * res[k].x + (double)res[k].y * res[k].y;
+      }
+    }
+    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
+    block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, sm);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launcher
+// ---------------------------------------------------------------------------
+int block_size_for(int N5, int LK) {
+  // blockDim = S * N5 with S a power of two and blockDim <= 256
+  int S = 1;
+  while (S * 2 * N5 <= 256) S *= 2;
+  (void)LK;
+  return N5 > 256 ? -1 : S * N5;
+}
+
+size_t dslash_smem_bytes(int P, int LK, int bd) {
+  size_t rb = (P == P64) ? 8 : 4;
+  size_t s = 0;
+  if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
+  s += 2 * (size_t)bd * 8;
+  return s;
+}
+
+template <int P, int LS, int LK>
+static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
+  const int bd = block_size_for(a.g.N5, LK);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const long long nb = (a.g.N + bd - 1) / bd;
+  const size_t sm = dslash_smem_bytes(P, LK, bd);
+  auto k = dslash_kernel<P, LS, LK>;
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  k<<<(unsigned)nb, bd, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st) {
+  const int LK = (a.l1.kind == LOC_SMAT || a.l2.kind == LOC_SMAT) ? LOC_SMAT : LOC_CLOVER;
+#define GBF_D(PP, LL)                                                     \
+  if (P == PP && LS == LL) {                                             \
+    if (LK == LOC_SMAT) return launch_t<PP, LL, LOC_SMAT>(a, st);        \
+    return launch_t<PP, LL, LOC_CLOVER>(a, st);                          \
+  }
+  GBF_D(P64, L64)
+  GBF_D(P32, L32)
+  GBF_D(P32, L32R)
+  GBF_D(P16, L32)
+  GBF_D(P16, L32R)
+#undef GBF_D
+  return cudaErrorInvalidValue;
+}
+
+// number of blocks a launch uses (reduction partial buffers are sized by it)
+long long dslash_blocks(const Geo& g, int LK) {
+  const int bd = block_size_for(g.N5, LK);
+  return (g.N + bd - 1) / bd;
+}
+
+}  // namespace gbf

@@ -1,0 +1,242 @@
+// gbf_kernels.cuh -- device building blocks shared by the kernel files:
+// site-local operators (clover, s-matrix), the deterministic block reduction
+// and its last-block finalisation, and the CG scalar updates.
+#pragma once
+#include "gbf_common.cuh"
+
+namespace gbf {
+
+// A site-local operator applied in a kernel epilogue.
+//   LOC_CLOVER: per 4D site two Hermitian 6x6 blocks (spins {0,1}, {2,3});
+//               72 reals per site: block b = 6 diagonal reals followed by the
+//               15 strictly-lower complex entries (row-major i > j).
+//               Storage per parity: FP64 double2 [36][Vh], FP32 float4 [18][Vh].
+//   LOC_SMAT:   one real Ls x Ls matrix per chirality acting on the s index,
+//               the same at every 4D site; [2][Ls][Ls] in the arithmetic type.
+//   LOC_SCALAR: multiplication by a real constant.
+struct LocalOp {
+  int kind;
+  const void* clov[2];  // per parity
+  const void* smat;
+  double scalar;
+};
+
+template <typename R> struct CloverLoad;
+template <> struct CloverLoad<double> {
+  static __device__ __forceinline__ void block(const void* base, int Vh, int cb, int b, double (&c)[36]) {
+    const double2* p = reinterpret_cast<const double2*>(base) + cb + (size_t)18 * b * Vh;
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+      double2 q = __ldg(p + (size_t)k * Vh);
+      c[2 * k] = q.x;
+      c[2 * k + 1] = q.y;
+    }
+  }
+};
+template <> struct CloverLoad<float> {
+  static __device__ __forceinline__ void block(const void* base, int Vh, int cb, int b, float (&c)[36]) {
+    const float4* p = reinterpret_cast<const float4*>(base) + cb + (size_t)9 * b * Vh;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      float4 q = __ldg(p + (size_t)k * Vh);
+      c[4 * k] = q.x; c[4 * k + 1] = q.y; c[4 * k + 2] = q.z; c[4 * k + 3] = q.w;
+    }
+  }
+};
+
+// off-diagonal index of (i, j), i > j
+__host__ __device__ constexpr int tri(int i, int j) { return i * (i - 1) / 2 + j; }
+
+template <typename R>
+__device__ __forceinline__ void clover_apply(const void* base, int Vh, int cb, cplx<R> (&v)[12]) {
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    R c[36];
+    CloverLoad<R>::block(base, Vh, cb, b, c);
+    cplx<R> o[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      cplx<R> acc = scl<R>(c[i], v[6 * b + i]);
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        if (j < i) {
+          const int t = tri(i, j);
+          acc = cmadd<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), v[6 * b + j]);
+        } else if (j > i) {
+          const int t = tri(j, i);
+          acc = cmaddc<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), v[6 * b + j]);
+        }
+      }
+      o[i] = acc;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) v[6 * b + i] = o[i];
+  }
+}
+
+// Per-thread local op (everything except LOC_SMAT, which needs the block).
+template <typename R>
+__device__ __forceinline__ void local_apply_thread(const LocalOp& l, int Vh, int parity, int cb, cplx<R> (&v)[12]) {
+  if (l.kind == LOC_CLOVER) {
+    clover_apply<R>(l.clov[parity], Vh, cb, v);
+  } else if (l.kind == LOC_SCALAR) {
+    const R s = (R)l.scalar;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[k] = scl<R>(s, v[k]);
+  }
+}
+
+// s-matrix op through shared memory.  Threads of one block hold complete
+// s-columns (blockDim is a multiple of N5, i5 = rhs*Ls + s fastest).
+// tile: 24*blockDim reals; mat: 2*Ls*Ls reals.  All threads must call.
+template <typename R>
+__device__ __forceinline__ void smat_apply_block(const R* mat_g, int Ls, R* tile, R* mat, cplx<R> (&v)[12], bool load_mat) {
+  const int t = threadIdx.x, bd = blockDim.x;
+  if (load_mat)
+    for (int k = t; k < 2 * Ls * Ls; k += bd) mat[k] = mat_g[k];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    tile[(2 * k) * bd + t] = v[k].x;
+    tile[(2 * k + 1) * bd + t] = v[k].y;
+  }
+  __syncthreads();
+  const int s = t % Ls;
+  const int base = t - s;
+  const R* m0 = mat + s * Ls;
+  const R* m1 = mat + Ls * Ls + s * Ls;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    const R* m = k < 6 ? m0 : m1;
+    R ax = 0, ay = 0;
+    for (int sp = 0; sp < Ls; ++sp) {
+      ax = fma(m[sp], tile[(2 * k) * bd + base + sp], ax);
+      ay = fma(m[sp], tile[(2 * k + 1) * bd + base + sp], ay);
+    }
+    v[k] = mk<R>(ax, ay);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reduction: block tree over sites (stride N5), per-rhs sum of
+// the s entries, per-block partials, last block sums the partials in block
+// order and applies a finaliser to the CG state.
+// ---------------------------------------------------------------------------
+enum Fin { FIN_STORE = 0, FIN_ALPHA = 1, FIN_BETA = 2, FIN_INIT = 3 };
+
+struct RedArgs {
+  int fin;
+  double2* partial;   // [gridDim][nrhs]
+  unsigned* counter;  // zero on entry, restored to zero by the last block
+  CGState* st;
+};
+
+__device__ __forceinline__ void finalize(const RedArgs& r, int rhs, double re, double im) {
+  CGState* st = r.st;
+  switch (r.fin) {
+    case FIN_STORE:
+      st->last[rhs] = re;
+      st->last_im[rhs] = im;
+      break;
+    case FIN_ALPHA: {
+      st->d[rhs] = re;
+      double a = 0.0;
+      if (!st->done[rhs]) {
+        if (!(re > 0.0) || !isfinite(re)) {
+          st->done[rhs] = 1;
+          st->breakdown = 1;
+        } else {
+          a = st->cp[rhs] / re;
+        }
+      }
+      st->alpha[rhs] = a;
+      break;
+    }
+    case FIN_BETA: {
+      if (!st->done[rhs]) {
+        double b = re / st->cp[rhs];
+        st->beta[rhs] = b;
+        st->cp[rhs] = re;
+        if (re <= st->rsq[rhs]) st->done[rhs] = 1;
+        if (!isfinite(re)) { st->done[rhs] = 1; st->breakdown = 1; }
+      } else {
+        st->beta[rhs] = 0.0;
+      }
+      break;
+    }
+    case FIN_INIT:
+      st->cp[rhs] = re;
+      st->alpha[rhs] = 0.0;
+      st->beta[rhs] = 0.0;
+      st->done[rhs] = (re <= st->rsq[rhs]) ? 1 : 0;
+      break;
+  }
+}
+
+// sm: 2*blockDim doubles of shared memory.  Every thread of the block calls.
+__device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double vre, double vim, int N5, int Ls, int nrhs, double* sm) {
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int S = bd / N5;  // power of two by construction
+  sm[t] = vre;
+  sm[bd + t] = vim;
+  __syncthreads();
+  for (int k = S >> 1; k >= 1; k >>= 1) {
+    if (t < k * N5) {
+      sm[t] += sm[t + k * N5];
+      sm[bd + t] += sm[bd + t + k * N5];
+    }
+    __syncthreads();
+  }
+  if (t < nrhs) {
+    double ar = 0, ai = 0;
+    for (int s = 0; s < Ls; ++s) {
+      ar += sm[t * Ls + s];
+      ai += sm[bd + t * Ls + s];
+    }
+    r.partial[(size_t)blockIdx.x * nrhs + t] = make_double2(ar, ai);
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ int s_last;
+  if (t == 0) s_last = (atomicAdd(r.counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  int P2 = 1;
+  while (P2 < bd) P2 <<= 1;
+  for (int rhs = 0; rhs < nrhs; ++rhs) {
+    double ar = 0, ai = 0;
+    for (unsigned b = t; b < gridDim.x; b += bd) {
+      double2 q = __ldcg(r.partial + (size_t)b * nrhs + rhs);
+      ar += q.x;
+      ai += q.y;
+    }
+    sm[t] = ar;
+    sm[bd + t] = ai;
+    __syncthreads();
+    for (int k = P2 >> 1; k >= 1; k >>= 1) {
+      if (t < k && t + k < bd) {
+        sm[t] += sm[t + k];
+        sm[bd + t] += sm[bd + t + k];
+      }
+      __syncthreads();
+    }
+    if (t == 0) finalize(r, rhs, sm[0], sm[bd]);
+    __syncthreads();
+  }
+  if (t == 0) {
+    if (r.fin == FIN_BETA || r.fin == FIN_INIT) {
+      int all = 1;
+      for (int rhs = 0; rhs < nrhs; ++rhs) all &= r.st->done[rhs];
+      if (r.fin == FIN_BETA) {
+        r.st->iter += 1;
+        if (r.st->iter >= r.st->maxiter) all = 1;
+      }
+      r.st->all_done = all;
+    }
+    *r.counter = 0;
+    __threadfence();
+  }
+}
+
+}  // namespace gbf

@@ -1,0 +1,90 @@
+// gbf_launch.cuh -- argument blocks and host launchers of the device kernels.
+#pragma once
+#include "gbf_kernels.cuh"
+
+namespace gbf {
+
+// Even-odd hopping kernel (gbf_dslash.cu):
+//   out = c1 * L1(Dhop_{p <- 1-p}(in)) + c2 * L2(X)  [+ reduction of <Y,out> or |out|^2]
+struct DslashArgs {
+  Geo g;
+  int out_parity;
+  float sgn;  // projector sign on the forward term: -1 Dhop, +1 Dhop^dag
+  const void* in;
+  void* out;
+  const void* links;
+  LocalOp l1, l2;  // l2 may not be LOC_SMAT
+  double c1, c2;
+  const void* X;
+  int red;  // 0 none, 1 <Y,out>, 2 |out|^2
+  const void* Y;
+  RedArgs ra;
+  int check_done;
+};
+cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st);
+int block_size_for(int N5, int LK);
+long long dslash_blocks(const Geo& g, int LK);
+
+// Site-local kernel on one parity (gbf_local.cu):
+//   if (pre):  W = A + beta_rhs * W   (beta from the CG state; written back)
+//   out = c1 * L(W or A) + c2 * X       [+ reduction as above on `out`]
+struct LocalArgs {
+  Geo g;
+  int parity;
+  const void* A;
+  void* W;       // pre-step target (p in CG), may be null
+  int pre;       // 1: W = A + beta*W before the op
+  LocalOp l;
+  void* out;
+  double c1, c2;
+  const void* X;
+  int red;
+  const void* Y;
+  RedArgs ra;
+  int check_done;
+};
+cudaError_t launch_local(int P, const LocalArgs& a, cudaStream_t st);
+
+// CG update (gbf_local.cu): r -= alpha*mmp; x += alpha*p; reduce |r|^2 -> FIN_BETA
+struct CGUpdateArgs {
+  Geo g;
+  void* r;
+  const void* mmp;
+  void* x;
+  const void* p;
+  RedArgs ra;
+};
+cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st);
+
+// Generic BLAS over one half field (gbf_local.cu):
+//   out = a_rhs * x + b_rhs * y  (a, b per rhs, from host arrays in the args)
+//   then optional reduction: 1 <Y,out>, 2 |out|^2, 3 <x, y> (no write)
+struct BlasArgs {
+  Geo g;
+  void* out;
+  const void* x;
+  const void* y;
+  double a_re[kMaxRhs], a_im[kMaxRhs], b_re[kMaxRhs];
+  int write;
+  int red;
+  RedArgs ra;
+};
+cudaError_t launch_blas(int P, const BlasArgs& a, cudaStream_t st);
+
+// precision conversion of a half field
+cudaError_t launch_convert(int Pout, void* out, int Pin, const void* in, long long N, double scale, cudaStream_t st);
+
+// CG state initialisation from the FIN_STORE result: rsq = eps^2 * last, cp = last
+cudaError_t launch_cg_init(CGState* st, int nrhs, double eps, int maxiter, cudaStream_t s);
+
+// natural <-> internal field transfer; natural = complex128 [V][Ls][12] of one rhs
+cudaError_t launch_import(int P, const Geo& g, const double2* nat, void* full, int rhs, int to_natural, cudaStream_t st);
+
+// gauge packing: natural complex128 [4][V][9] on the device -> internal links
+cudaError_t launch_pack_links(int LS, const Geo& g, const double2* U, void* links, const double* lam_mu, const double* ph,
+                              unsigned* err_bits, cudaStream_t st);
+// clover: natural gauge -> per parity clover and inverse (FP64 double2[36][Vh] and FP32 float4[18][Vh])
+cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double csw_r, double csw_t, void* c64, void* ci64,
+                          void* c32, void* ci32, unsigned* err_bits, cudaStream_t st);
+
+}  // namespace gbf

@@ -1,0 +1,597 @@
+// gbf_local.cu -- site-local kernels: clover / s-matrix application, the CG
+// vector updates, BLAS with deterministic reductions, precision conversion,
+// natural <-> internal layout transfer, gauge packing and the clover build.
+//
+// All of these are HBM-bound streaming kernels (bytes per 5D site listed at
+// each kernel); the clover build is a one-time set-up kernel.
+#include "gbf_launch.cuh"
+
+namespace gbf {
+
+// ---------------------------------------------------------------------------
+// site-local op with optional CG pre-step (p = r + beta p):
+// bytes/site: A + (W read+write if pre) + out + (X) + clover (288 B FP32, 576 B FP64)
+// ---------------------------------------------------------------------------
+template <int P, int LK>
+__global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  extern __shared__ double smem_d[];
+  const Geo& g = a.g;
+  if (a.check_done && a.ra.st->all_done) return;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = n < g.N;
+  V v[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) v[k] = cz<R>();
+  int cb = 0;
+  if (active) {
+    cb = (int)(n / g.N5);
+    load_spinor<P>(a.A, g.N, n, v);
+    if (a.pre) {
+      const int rhs = (int)(n - (long long)cb * g.N5) / g.Ls;
+      const R beta = (R)a.ra.st->beta[rhs];
+      V w[12];
+      load_spinor<P>(a.W, g.N, n, w);
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[k] = mk<R>(fma(beta, w[k].x, v[k].x), fma(beta, w[k].y, v[k].y));
+      store_spinor<P>(a.W, g.N, n, v);
+    }
+  }
+  if (LK == LOC_SMAT) {
+    if (a.l.kind == LOC_SMAT) {
+      R* tile = reinterpret_cast<R*>(smem_d);
+      R* mat = tile + 24 * blockDim.x;
+      smat_apply_block<R>(reinterpret_cast<const R*>(a.l.smat), g.Ls, tile, mat, v, true);
+    }
+  } else if (active && a.l.kind != LOC_NONE) {
+    local_apply_thread<R>(a.l, g.Vh, a.parity, cb, v);
+  }
+  if (active) {
+    if (a.c1 != 1.0) {
+      const R c1 = (R)a.c1;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[k] = scl<R>(c1, v[k]);
+    }
+    if (a.X) {
+      V xv[12];
+      load_spinor<P>(a.X, g.N, n, xv);
+      const R c2 = (R)a.c2;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[k] = mk<R>(fma(c2, xv[k].x, v[k].x), fma(c2, xv[k].y, v[k].y));
+    }
+    if (a.out) store_spinor<P>(a.out, g.N, n, v);
+  }
+  if (a.red) {
+    double vr = 0, vi = 0;
+    if (active) {
+      if (a.red == 1) {
+        V yv[12];
+        load_spinor<P>(a.Y, g.N, n, yv);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+          vr += (double)yv[k].x * v[k].x + (double)yv[k].y * v[k].y;
+          vi += (double)yv[k].x * v[k].y - (double)yv[k].y * v[k].x;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) vr += (double)v[k].x * v[k].x + (double)v[k].y * v[k].y;
+      }
+    }
+    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
+    block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, sm);
+  }
+}
+
+static size_t local_smem(int P, int LK, int bd) {
+  size_t rb = (P == P64) ? 8 : 4;
+  size_t s = 0;
+  if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
+  return s + 2 * (size_t)bd * 8;
+}
+
+template <int P, int LK>
+static cudaError_t launch_local_t(const LocalArgs& a, cudaStream_t st) {
+  const int bd = block_size_for(a.g.N5, LK);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const long long nb = (a.g.N + bd - 1) / bd;
+  const size_t sm = local_smem(P, LK, bd);
+  auto k = local_kernel<P, LK>;
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  k<<<(unsigned)nb, bd, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_local(int P, const LocalArgs& a, cudaStream_t st) {
+  const bool sm = a.l.kind == LOC_SMAT;
+  if (P == P64) return sm ? launch_local_t<P64, LOC_SMAT>(a, st) : launch_local_t<P64, LOC_CLOVER>(a, st);
+  if (P == P32) return sm ? launch_local_t<P32, LOC_SMAT>(a, st) : launch_local_t<P32, LOC_CLOVER>(a, st);
+  if (P == P16) return sm ? launch_local_t<P16, LOC_SMAT>(a, st) : launch_local_t<P16, LOC_CLOVER>(a, st);
+  return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// CG update: r -= alpha mmp; x += alpha p; |r|^2 -> beta, convergence.
+// bytes/site: r, mmp, x, p read + r, x written = 6 spinors
+// ---------------------------------------------------------------------------
+template <int P>
+__global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  extern __shared__ double smem_d[];
+  const Geo& g = a.g;
+  if (a.ra.st->all_done) return;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double vr = 0;
+  if (n < g.N) {
+    const int i5 = (int)(n % g.N5);
+    const int rhs = i5 / g.Ls;
+    const R al = (R)a.ra.st->alpha[rhs];
+    V r[12], m[12], x[12], p[12];
+    load_spinor<P>(a.r, g.N, n, r);
+    load_spinor<P>(a.mmp, g.N, n, m);
+    load_spinor<P>(a.x, g.N, n, x);
+    load_spinor<P>(a.p, g.N, n, p);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      r[k] = mk<R>(fma(-al, m[k].x, r[k].x), fma(-al, m[k].y, r[k].y));
+      x[k] = mk<R>(fma(al, p[k].x, x[k].x), fma(al, p[k].y, x[k].y));
+      vr += (double)r[k].x * r[k].x + (double)r[k].y * r[k].y;
+    }
+    store_spinor<P>(a.r, g.N, n, r);
+    store_spinor<P>(a.x, g.N, n, x);
+  }
+  block_reduce_finalize(a.ra, vr, 0.0, g.N5, g.Ls, g.nrhs, smem_d);
+}
+
+cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st) {
+  const int bd = block_size_for(a.g.N5, LOC_NONE);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const long long nb = (a.g.N + bd - 1) / bd;
+  const size_t sm = 2 * (size_t)bd * 8;
+  if (P == P64) cg_update_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
+  else if (P == P32) cg_update_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
+  else if (P == P16) cg_update_kernel<P16><<<(unsigned)nb, bd, sm, st>>>(a);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// BLAS: out = a x + b y (complex a, real b, per rhs), reductions
+// ---------------------------------------------------------------------------
+template <int P>
+__global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  extern __shared__ double smem_d[];
+  const Geo& g = a.g;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double vr = 0, vi = 0;
+  if (n < g.N) {
+    const int i5 = (int)(n % g.N5);
+    const int rhs = i5 / g.Ls;
+    V x[12], y[12], o[12];
+    load_spinor<P>(a.x, g.N, n, x);
+    if (a.y) load_spinor<P>(a.y, g.N, n, y);
+    else
+#pragma unroll
+      for (int k = 0; k < 12; ++k) y[k] = cz<R>();
+    if (a.red == 3) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        vr += (double)x[k].x * y[k].x + (double)x[k].y * y[k].y;
+        vi += (double)x[k].x * y[k].y - (double)x[k].y * y[k].x;
+      }
+    } else {
+      const V ac = mk<R>((R)a.a_re[rhs], (R)a.a_im[rhs]);
+      const R bc = (R)a.b_re[rhs];
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        V t = cmul<R>(ac, x[k]);
+        o[k] = mk<R>(fma(bc, y[k].x, t.x), fma(bc, y[k].y, t.y));
+      }
+      if (a.write) store_spinor<P>(a.out, g.N, n, o);
+      if (a.red == 2)
+#pragma unroll
+        for (int k = 0; k < 12; ++k) vr += (double)o[k].x * o[k].x + (double)o[k].y * o[k].y;
+    }
+  }
+  if (a.red) block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, smem_d);
+}
+
+cudaError_t launch_blas(int P, const BlasArgs& a, cudaStream_t st) {
+  const int bd = block_size_for(a.g.N5, LOC_NONE);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const long long nb = (a.g.N + bd - 1) / bd;
+  const size_t sm = 2 * (size_t)bd * 8;
+  if (P == P64) blas_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
+  else if (P == P32) blas_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
+  else if (P == P16) blas_kernel<P16><<<(unsigned)nb, bd, sm, st>>>(a);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// precision conversion
+// ---------------------------------------------------------------------------
+template <int PO, int PI>
+__global__ void convert_kernel(void* out, const void* in, long long N, double scale) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  using RI = typename SpinorT<PI>::R;
+  using RO = typename SpinorT<PO>::R;
+  cplx<RI> v[12];
+  load_spinor<PI>(in, N, n, v);
+  cplx<RO> o[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) o[k] = mk<RO>((RO)(scale * (double)v[k].x), (RO)(scale * (double)v[k].y));
+  store_spinor<PO>(out, N, n, o);
+}
+
+cudaError_t launch_convert(int Pout, void* out, int Pin, const void* in, long long N, double scale, cudaStream_t st) {
+  const int bd = 256;
+  const unsigned nb = (unsigned)((N + bd - 1) / bd);
+#define GBF_CV(A, B) \
+  if (Pout == A && Pin == B) { convert_kernel<A, B><<<nb, bd, 0, st>>>(out, in, N, scale); return cudaGetLastError(); }
+  GBF_CV(P64, P64) GBF_CV(P64, P32) GBF_CV(P64, P16)
+  GBF_CV(P32, P64) GBF_CV(P32, P32) GBF_CV(P32, P16)
+  GBF_CV(P16, P64) GBF_CV(P16, P32) GBF_CV(P16, P16)
+#undef GBF_CV
+  return cudaErrorInvalidValue;
+}
+
+__global__ void cg_init_kernel(CGState* st, int nrhs, double eps, int maxiter) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int all = 1;
+  st->nrhs = nrhs;
+  st->iter = 0;
+  st->breakdown = 0;
+  st->maxiter = maxiter;
+  for (int r = 0; r < nrhs; ++r) {
+    const double ssq = st->last[r];
+    st->cp[r] = ssq;
+    st->rsq[r] = eps * eps * ssq;
+    st->alpha[r] = 0.0;
+    st->beta[r] = 0.0;
+    st->done[r] = (ssq == 0.0) ? 1 : 0;
+    all &= st->done[r];
+  }
+  st->all_done = all;
+}
+
+cudaError_t launch_cg_init(CGState* st, int nrhs, double eps, int maxiter, cudaStream_t s) {
+  cg_init_kernel<<<1, 32, 0, s>>>(st, nrhs, eps, maxiter);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// natural <-> internal: natural = complex128 [V][Ls][12] (site lexicographic,
+// x0 fastest; s fastest within a site); internal full field [even][odd].
+// ---------------------------------------------------------------------------
+template <int P>
+__global__ void import_kernel(Geo g, const double2* nat, void* full, int rhs, int to_natural) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long V = 2LL * g.Vh;
+  if (t >= V * g.Ls) return;
+  const long long xs = t / g.Ls;
+  const int s = (int)(t - xs * g.Ls);
+  int x[4];
+  long long r = xs;
+  for (int m = 0; m < 4; ++m) { x[m] = (int)(r % g.L[m]); r /= g.L[m]; }
+  const int par = (x[0] + x[1] + x[2] + x[3]) & 1;
+  const int cb = cb_index(g, x);
+  const long long n = (long long)cb * g.N5 + (long long)rhs * g.Ls + s;
+  using R = typename SpinorT<P>::R;
+  char* half = reinterpret_cast<char*>(full) + (par ? half_bytes(P, g.N) : 0);
+  const double2* src = nat + (size_t)t * 12;
+  cplx<R> v[12];
+  if (!to_natural) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[k] = mk<R>((R)src[k].x, (R)src[k].y);
+    store_spinor<P>(half, g.N, n, v);
+  } else {
+    load_spinor<P>(half, g.N, n, v);
+    double2* dst = const_cast<double2*>(src);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) dst[k] = make_double2((double)v[k].x, (double)v[k].y);
+  }
+}
+
+cudaError_t launch_import(int P, const Geo& g, const double2* nat, void* full, int rhs, int to_natural, cudaStream_t st) {
+  const long long tot = 2LL * g.Vh * g.Ls;
+  const unsigned nb = (unsigned)((tot + 255) / 256);
+  if (P == P64) import_kernel<P64><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
+  else if (P == P32) import_kernel<P32><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
+  else if (P == P16) import_kernel<P16><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// gauge packing
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+
+__device__ void atomic_max_err(unsigned* e, double v) {
+  float f = (float)fmin(v, 3.0e38);
+  if (!(f >= 0.f)) f = 3.0e38f;  // NaN
+  atomicMax(e, __float_as_uint(f));
+}
+
+// per-direction link factor: lam = -cc_mu/2 and the boundary phase (re, im)
+struct LamPh {
+  double lam, re, im;
+};
+
+template <int LS>
+__global__ void pack_links_kernel(Geo g, const double2* U, void* links, LamPh lam_ph0, LamPh lam_ph1, LamPh lam_ph2,
+                                  LamPh lam_ph3, unsigned* err) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long V = 2LL * g.Vh;
+  if (t >= 4 * V) return;
+  const int mu = (int)(t / V);
+  const long long xs = t - (long long)mu * V;
+  int x[4];
+  long long r = xs;
+  for (int m = 0; m < 4; ++m) { x[m] = (int)(r % g.L[m]); r /= g.L[m]; }
+  const int par = (x[0] + x[1] + x[2] + x[3]) & 1;
+  const int cb = cb_index(g, x);
+  double2 u[9];
+  for (int k = 0; k < 9; ++k) u[k] = U[(size_t)t * 9 + k];
+  const LamPh lp = mu == 0 ? lam_ph0 : mu == 1 ? lam_ph1 : mu == 2 ? lam_ph2 : lam_ph3;
+  if (LS == L32R) {
+    // unitarity and det = 1 check for the 12-real storage
+    double e = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double2 s = make_double2(0, 0);
+        for (int k = 0; k < 3; ++k) {
+          double2 q = zmul(zconj(u[3 * k + i]), u[3 * k + j]);
+          s.x += q.x; s.y += q.y;
+        }
+        if (i == j) s.x -= 1.0;
+        e = fmax(e, fabs(s.x) + fabs(s.y));
+      }
+    double2 c0 = zmul(u[4], u[8]), c1 = zmul(u[5], u[7]);
+    double2 m0 = make_double2(c0.x - c1.x, c0.y - c1.y);
+    double2 c2 = zmul(u[3], u[8]), c3 = zmul(u[5], u[6]);
+    double2 m1 = make_double2(c2.x - c3.x, c2.y - c3.y);
+    double2 c4 = zmul(u[3], u[7]), c5 = zmul(u[4], u[6]);
+    double2 m2 = make_double2(c4.x - c5.x, c4.y - c5.y);
+    double2 a0 = zmul(u[0], m0), a1 = zmul(u[1], m1), a2 = zmul(u[2], m2);
+    double2 det = make_double2(a0.x - a1.x + a2.x, a0.y - a1.y + a2.y);
+    e = fmax(e, fabs(det.x - 1.0) + fabs(det.y));
+    atomic_max_err(err, e);
+    float4* b = reinterpret_cast<float4*>(links) + (size_t)(par * 4 + mu) * 3 * g.Vh + cb;
+    b[0] = make_float4((float)u[0].x, (float)u[0].y, (float)u[1].x, (float)u[1].y);
+    b[g.Vh] = make_float4((float)u[2].x, (float)u[2].y, (float)u[3].x, (float)u[3].y);
+    b[2 * (size_t)g.Vh] = make_float4((float)u[4].x, (float)u[4].y, (float)u[5].x, (float)u[5].y);
+    return;
+  }
+  double2 lam = make_double2(lp.lam, 0.0);
+  if (x[mu] == g.L[mu] - 1) lam = make_double2(lp.lam * lp.re, lp.lam * lp.im);
+  for (int k = 0; k < 9; ++k) u[k] = zmul(lam, u[k]);
+  if (LS == L64) {
+    double2* b = reinterpret_cast<double2*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
+    for (int k = 0; k < 9; ++k) b[(size_t)k * g.Vh] = u[k];
+  } else {
+    float2* b = reinterpret_cast<float2*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
+    for (int k = 0; k < 9; ++k) b[(size_t)k * g.Vh] = make_float2((float)u[k].x, (float)u[k].y);
+  }
+}
+
+cudaError_t launch_pack_links(int LS, const Geo& g, const double2* U, void* links, const double* lam_mu, const double* ph,
+                              unsigned* err, cudaStream_t st) {
+  const long long tot = 8LL * g.Vh;
+  const unsigned nb = (unsigned)((tot + 255) / 256);
+  LamPh lp[4];
+  for (int m = 0; m < 4; ++m) lp[m] = LamPh{lam_mu[m], ph[2 * m], ph[2 * m + 1]};
+  if (LS == L64) pack_links_kernel<L64><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
+  else if (LS == L32) pack_links_kernel<L32><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
+  else if (LS == L32R) pack_links_kernel<L32R><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// clover build (one thread per 4D site, FP64):
+//   F_munu = 1/8 (Q - Q^+), Q the four-leaf clover (lib/gpt/qcd/gauge/loops.py:162-174)
+//   C = sum_{mu<nu} -1/2 c_p sigma_munu (x) F_munu + diag   (reference/wilson_clover.py:91-127)
+// sigma_munu restricted to the chiral blocks comes from the host.
+// ---------------------------------------------------------------------------
+struct SigmaBlocks {
+  double2 s[6][2][4];  // [plane][block][2x2]
+};
+
+__device__ __forceinline__ void m3mul(const double2* a, const double2* b, double2* c) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double2 s = make_double2(0, 0);
+      for (int k = 0; k < 3; ++k) {
+        double2 q = zmul(a[3 * i + k], b[3 * k + j]);
+        s.x += q.x; s.y += q.y;
+      }
+      c[3 * i + j] = s;
+    }
+}
+__device__ __forceinline__ void m3adj(const double2* a, double2* c) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) c[3 * i + j] = zconj(a[3 * j + i]);
+}
+
+struct NatGeo {
+  int L[4];
+  __device__ long long idx(const int (&x)[4]) const { return x[0] + (long long)L[0] * (x[1] + (long long)L[1] * (x[2] + (long long)L[2] * x[3])); }
+  __device__ long long shift(long long s, int mu, int d) const {
+    int x[4];
+    long long r = s;
+    for (int m = 0; m < 4; ++m) { x[m] = (int)(r % L[m]); r /= L[m]; }
+    x[mu] = (x[mu] + d + L[mu]) % L[mu];
+    return idx(x);
+  }
+};
+
+__device__ void vfield(const NatGeo& G, const double2* U, long long V, int mu, int nu, long long y, double2* out) {
+  auto L = [&](int m, long long s) { return U + ((size_t)m * V + s) * 9; };
+  double2 p[9], q[9], r9[9], su[9], sd[9];
+  // staple_up(y) = U_nu(y+mu) U_mu(y+nu)^+ U_nu(y)^+
+  m3adj(L(mu, G.shift(y, nu, 1)), p);
+  m3mul(L(nu, G.shift(y, mu, 1)), p, q);
+  m3adj(L(nu, y), p);
+  m3mul(q, p, su);
+  // staple_down(y) = U_nu(z+mu)^+ U_mu(z)^+ U_nu(z), z = y - nu
+  long long z = G.shift(y, nu, -1);
+  m3adj(L(nu, G.shift(z, mu, 1)), p);
+  m3adj(L(mu, z), q);
+  m3mul(p, q, r9);
+  m3mul(r9, L(nu, z), sd);
+  for (int e = 0; e < 9; ++e) out[e] = make_double2(su[e].x - sd[e].x, su[e].y - sd[e].y);
+}
+
+__device__ bool invert6(double2 (&A)[36], double2 (&I)[36]) {
+  for (int i = 0; i < 36; ++i) I[i] = make_double2((i % 7 == 0) ? 1.0 : 0.0, 0.0);
+  for (int col = 0; col < 6; ++col) {
+    int piv = col;
+    double best = -1;
+    for (int r = col; r < 6; ++r) {
+      double m = A[6 * r + col].x * A[6 * r + col].x + A[6 * r + col].y * A[6 * r + col].y;
+      if (m > best) { best = m; piv = r; }
+    }
+    if (!(best > 0)) return false;
+    if (piv != col)
+      for (int k = 0; k < 6; ++k) {
+        double2 t = A[6 * col + k]; A[6 * col + k] = A[6 * piv + k]; A[6 * piv + k] = t;
+        t = I[6 * col + k]; I[6 * col + k] = I[6 * piv + k]; I[6 * piv + k] = t;
+      }
+    double2 pv = A[6 * col + col];
+    double pn = pv.x * pv.x + pv.y * pv.y;
+    double2 pinv = make_double2(pv.x / pn, -pv.y / pn);
+    for (int k = 0; k < 6; ++k) { A[6 * col + k] = zmul(A[6 * col + k], pinv); I[6 * col + k] = zmul(I[6 * col + k], pinv); }
+    for (int r = 0; r < 6; ++r) {
+      if (r == col) continue;
+      double2 f = A[6 * r + col];
+      for (int k = 0; k < 6; ++k) {
+        double2 a = zmul(f, A[6 * col + k]), b = zmul(f, I[6 * col + k]);
+        A[6 * r + k] = make_double2(A[6 * r + k].x - a.x, A[6 * r + k].y - a.y);
+        I[6 * r + k] = make_double2(I[6 * r + k].x - b.x, I[6 * r + k].y - b.y);
+      }
+    }
+  }
+  return true;
+}
+
+__device__ void store_clover_block(const double2 (&M)[36], int b, int cb, int Vh, double2* c64, float4* c32) {
+  double re[36];
+  for (int i = 0; i < 6; ++i) re[i] = M[7 * i].x;
+  for (int i = 1; i < 6; ++i)
+    for (int j = 0; j < i; ++j) {
+      re[6 + 2 * tri(i, j)] = M[6 * i + j].x;
+      re[6 + 2 * tri(i, j) + 1] = M[6 * i + j].y;
+    }
+  for (int k = 0; k < 18; ++k) c64[(size_t)(18 * b + k) * Vh + cb] = make_double2(re[2 * k], re[2 * k + 1]);
+  for (int k = 0; k < 9; ++k)
+    c32[(size_t)(9 * b + k) * Vh + cb] = make_float4((float)re[4 * k], (float)re[4 * k + 1], (float)re[4 * k + 2], (float)re[4 * k + 3]);
+}
+
+__global__ void clover_kernel(Geo g, const double2* U, SigmaBlocks sig, double diag, double csw_r, double csw_t, double2* c64,
+                              double2* ci64, float4* c32, float4* ci32, unsigned* err) {
+  const long long xs = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long V = 2LL * g.Vh;
+  if (xs >= V) return;
+  NatGeo G;
+  for (int m = 0; m < 4; ++m) G.L[m] = g.L[m];
+  int x[4];
+  long long r = xs;
+  for (int m = 0; m < 4; ++m) { x[m] = (int)(r % g.L[m]); r /= g.L[m]; }
+  const int par = (x[0] + x[1] + x[2] + x[3]) & 1;
+  const int cb = cb_index(g, x);
+  double2 blk[2][36];
+  for (int b = 0; b < 2; ++b)
+    for (int e = 0; e < 36; ++e) blk[b][e] = make_double2(e % 7 == 0 ? diag : 0.0, 0.0);
+  int plane = 0;
+  for (int mu = 0; mu < 4; ++mu)
+    for (int nu = mu + 1; nu < 4; ++nu, ++plane) {
+      const double cp = (nu == 3) ? csw_t : csw_r;
+      if (cp == 0.0) continue;
+      double2 v[9], t1[9], t2[9], F[9];
+      vfield(G, U, V, mu, nu, xs, v);
+      m3mul(U + ((size_t)mu * V + xs) * 9, v, t1);
+      const long long xm = G.shift(xs, mu, -1);
+      vfield(G, U, V, mu, nu, xm, v);
+      m3mul(v, U + ((size_t)mu * V + xm) * 9, t2);
+      for (int e = 0; e < 9; ++e) t1[e] = make_double2(t1[e].x + t2[e].x, t1[e].y + t2[e].y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double2 d = zconj(t1[3 * j + i]);
+          F[3 * i + j] = make_double2(0.125 * (t1[3 * i + j].x - d.x), 0.125 * (t1[3 * i + j].y - d.y));
+        }
+      for (int b = 0; b < 2; ++b)
+        for (int s1 = 0; s1 < 2; ++s1)
+          for (int s2 = 0; s2 < 2; ++s2) {
+            double2 sg = sig.s[plane][b][2 * s1 + s2];
+            if (sg.x == 0.0 && sg.y == 0.0) continue;
+            double2 f = make_double2(-0.5 * cp * sg.x, -0.5 * cp * sg.y);
+            for (int a = 0; a < 3; ++a)
+              for (int c = 0; c < 3; ++c) {
+                double2 q = zmul(f, F[3 * a + c]);
+                double2& e = blk[b][6 * (3 * s1 + a) + (3 * s2 + c)];
+                e.x += q.x;
+                e.y += q.y;
+              }
+          }
+    }
+  const size_t poff36 = (size_t)par * 36 * g.Vh, poff18 = (size_t)par * 18 * g.Vh;
+  for (int b = 0; b < 2; ++b) {
+    store_clover_block(blk[b], b, cb, g.Vh, c64 + poff36, c32 + poff18);
+    double2 A[36], I[36];
+    for (int e = 0; e < 36; ++e) A[e] = blk[b][e];
+    if (!invert6(A, I)) atomic_max_err(err, 1e30);
+    store_clover_block(I, b, cb, g.Vh, ci64 + poff36, ci32 + poff18);
+  }
+}
+
+cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double csw_r, double csw_t, void* c64, void* ci64,
+                          void* c32, void* ci32, unsigned* err, cudaStream_t st) {
+  // sigma_munu = 1/2 [g_mu, g_nu] in the chiral blocks, from the sparse gamma tables
+  SigmaBlocks sig;
+  auto gm = [](int mu, int r, int c) -> double2 {
+    if (gperm(mu, r) != c) return make_double2(0, 0);
+    switch (gcoef(mu, r)) {
+      case 0: return make_double2(1, 0);
+      case 1: return make_double2(-1, 0);
+      case 2: return make_double2(0, 1);
+      default: return make_double2(0, -1);
+    }
+  };
+  int plane = 0;
+  for (int mu = 0; mu < 4; ++mu)
+    for (int nu = mu + 1; nu < 4; ++nu, ++plane) {
+      double2 S[16];
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+          double re = 0, im = 0;
+          for (int k = 0; k < 4; ++k) {
+            double2 a = gm(mu, i, k), b = gm(nu, k, j), c = gm(nu, i, k), d = gm(mu, k, j);
+            re += (a.x * b.x - a.y * b.y) - (c.x * d.x - c.y * d.y);
+            im += (a.x * b.y + a.y * b.x) - (c.x * d.y + c.y * d.x);
+          }
+          S[4 * i + j] = make_double2(0.5 * re, 0.5 * im);
+        }
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+          if ((i < 2) != (j < 2) && (S[4 * i + j].x != 0 || S[4 * i + j].y != 0)) return cudaErrorInvalidValue;
+      for (int b = 0; b < 2; ++b)
+        for (int s1 = 0; s1 < 2; ++s1)
+          for (int s2 = 0; s2 < 2; ++s2) sig.s[plane][b][2 * s1 + s2] = S[4 * (2 * b + s1) + (2 * b + s2)];
+    }
+  const long long V = 2LL * g.Vh;
+  const unsigned nb = (unsigned)((V + 127) / 128);
+  clover_kernel<<<nb, 128, 0, st>>>(g, U, sig, diag, csw_r, csw_t, (double2*)c64, (double2*)ci64, (float4*)c32, (float4*)ci32, err);
+  return cudaGetLastError();
+}
+
+}  // namespace gbf

@@ -1,0 +1,278 @@
+"""Fermion operators: g.qcd.fermion.wilson_clover and g.qcd.fermion.mobius.
+
+Mirrors lib/gpt/qcd/fermion/wilson.py:63-96 (parameter handling, kappa ->
+mass), lib/gpt/qcd/fermion/mobius.py:25-117 and the operator object of
+lib/gpt/qcd/fermion/operator/base.py:28-306 (method names, .converted(),
+.updated(), .propagator(), .even_odd_sites_decomposed()).  Every method maps
+to an opcode of the native library (lib/gpt/qcd/fermion/operator/interface.py:88-91
+-> cgpt apply_fermion_operator), here gbf_apply of libgbferm.so.
+"""
+import copy as _copy
+import ctypes
+
+import numpy as np
+
+from .. import _lib
+from .. import core
+from .gauge import gauge_field
+
+
+class matrix_operator:
+    """A linear map dst = A(src) on lattices, with optional adjoint/inverse."""
+
+    def __init__(self, mat, adj_mat=None, inv_mat=None, adj_inv_mat=None, otype=None):
+        self.mat = mat
+        self.adj_mat = adj_mat
+        self.inv_mat = inv_mat
+        self.adj_inv_mat = adj_inv_mat
+
+    def __call__(self, first, second=None):
+        if second is None:
+            src = first
+            dst = self._new_dst(src)
+            self.mat(dst, src)
+            return dst
+        self.mat(first, second)
+        return first
+
+    def _new_dst(self, src):
+        return src.new()
+
+    def __mul__(self, src):
+        return self(src)
+
+    def adj(self):
+        return matrix_operator(self.adj_mat, self.mat, self.adj_inv_mat, self.inv_mat)
+
+    def inv(self):
+        return matrix_operator(self.inv_mat, self.adj_inv_mat, self.mat, self.adj_mat)
+
+
+def _params_struct(name, p, dims, Ls, n_rhs):
+    s = _lib.gbf_params()
+    for i in range(4):
+        s.dims[i] = dims[i]
+    s.Ls = Ls
+    s.n_rhs = n_rhs
+    ph = p.get("boundary_phases", [1, 1, 1, 1])
+    for mu in range(4):
+        s.boundary_phases[2 * mu] = complex(ph[mu]).real
+        s.boundary_phases[2 * mu + 1] = complex(ph[mu]).imag
+    s.reconstruct = int(p.get("reconstruct", -1))
+    if name == "wilson_clover":
+        s.mass = float(p["mass"])
+        s.csw_r = float(p.get("csw_r", 0.0))
+        s.csw_t = float(p.get("csw_t", 0.0))
+        s.xi_0 = float(p.get("xi_0", 1.0) or 1.0)
+        s.nu = float(p.get("nu", 1.0) or 1.0)
+        s.isAnisotropic = int(bool(p.get("isAnisotropic", False)))
+    else:
+        s.mass_plus = float(p["mass_plus"])
+        s.mass_minus = float(p["mass_minus"])
+        s.b = float(p["b"])
+        s.c = float(p["c"])
+        s.M5 = float(p["M5"])
+        s.xi_0 = s.nu = 1.0
+    return s
+
+
+class fermion_operator(matrix_operator):
+    """Native fermion operator (cgpt_fermion_operator analogue)."""
+
+    def __init__(self, name, U, params, precision=None, daggered=False):
+        self.name = name
+        self.U = U
+        self.params = dict(params)
+        self.daggered = daggered
+        prec = precision if precision is not None else U.grid.precision
+        self.U_grid = U.grid.converted(prec)
+        self.precision = prec
+        self.Ls = int(params.get("Ls", 1)) if name == "mobius" else 1
+        self.n_rhs = int(params.get("n_rhs", 1))
+        dims = self.U_grid.fdimensions
+        self.F_layout = core.layout.get(self.U_grid, self.Ls, self.n_rhs, five_d=name == "mobius")
+        self.U_layout = core.layout.get(self.U_grid, 1, self.n_rhs, five_d=False)
+        L = _lib.load()
+        s = _params_struct(name, self.params, dims, self.Ls, self.n_rhs)
+        h = ctypes.c_void_p()
+        _lib.check(L.gbf_create(name.encode(), prec.code, ctypes.byref(s), ctypes.byref(h)))
+        self.obj = h
+        _lib.check(L.gbf_update_gauge(self.obj, U.U.ctypes.data_as(ctypes.c_void_p), 0, core.stream_ptr()))
+        self._register()
+
+    def __del__(self):
+        try:
+            if getattr(self, "obj", None) is not None:
+                _lib.load().gbf_delete(self.obj)
+                self.obj = None
+        except Exception:
+            pass
+
+    # ---- fields ----
+    def F_lattice(self, cb=core.full):
+        return core.lattice(self.F_layout, cb)
+
+    def U_lattice(self, cb=core.full):
+        return core.lattice(self.U_layout, cb)
+
+    # ---- opcode application (interface.py:88-91) ----
+    def _apply(self, opname, dst, src):
+        code = _lib.OPCODES[opname]
+        sp = src.cb.code
+        _lib.check(_lib.load().gbf_apply(self.obj, code, _lib.ptrs([src.ptr]), _lib.ptrs([dst.ptr]), 1, sp, core.stream_ptr()))
+        if opname in ("Meooe", "MeooeDag", "DhopEO", "DhopEODag"):
+            dst.cb = src.cb.inv()
+        elif src.cb is not core.full:
+            dst.cb = src.cb
+
+    def _op(self, name, name_dag, new_dst=None, inv=None, inv_dag=None):
+        def m(n):
+            return (lambda dst, src: self._apply(n, dst, src)) if n else None
+
+        a, ad, i, idg = m(name), m(name_dag), m(inv), m(inv_dag)
+        if self.daggered:
+            a, ad, i, idg = ad, a, idg, i
+        op = matrix_operator(a, ad, i, idg)
+        if new_dst is not None:
+            op._new_dst = new_dst
+        return op
+
+    def _register(self):
+        # base.py:84-169 (method registry)
+        self.M = self._op("M", "Mdag")
+        self.mat = self.M.mat
+        self.adj_mat = self.M.adj_mat
+        self.inv_mat = None
+        self.adj_inv_mat = None
+        self.Meooe = self._op("Meooe", "MeooeDag")
+        self.Mooee = self._op("Mooee", "MooeeDag", inv="MooeeInv", inv_dag="MooeeInvDag")
+        self.DhopEO = self._op("DhopEO", "DhopEODag")
+        self.Dhop = self._op("Dhop", "DhopDag")
+        self.Mdiag = self._op("Mdiag", None)
+        self.Dminus = self._op("Dminus", "DminusDag")
+        to_F = lambda src: self.F_lattice()
+        to_U = lambda src: self.U_lattice()
+        self.ImportPhysicalFermionSource = self._op("ImportPhysicalFermionSource", None, new_dst=to_F)
+        self.ExportPhysicalFermionSolution = self._op("ExportPhysicalFermionSolution", None, new_dst=to_U)
+
+    # ---- base.py:219-260 ----
+    def converted(self, precision):
+        return type(self)(self.U, self.params, precision=precision, daggered=self.daggered)
+
+    def updated(self, U):
+        return type(self)(U, self.params, precision=self.precision, daggered=self.daggered)
+
+    def adj(self):
+        return type(self)(self.U, self.params, precision=self.precision, daggered=not self.daggered)
+
+    def propagator(self, solver):
+        """base.py:270-286: Export * solver(op) * Import."""
+        exp, imp = self.ExportPhysicalFermionSolution, self.ImportPhysicalFermionSource
+        inv_matrix = solver(self)
+
+        def prop(dst, src):
+            t = imp(src)
+            x = inv_matrix(t)
+            exp(dst, x)
+
+        return matrix_operator(prop)
+
+    def even_odd_sites_decomposed(self, parity):
+        return _even_odd_sites(self, parity)
+
+    def link_bytes(self):
+        """Bytes per stored link (144 FP64, 72 FP32, 48 FP32 reconstruct-12)."""
+        return _lib.load().gbf_link_bytes(self.obj)
+
+    # native eo2_ne + CG on the device (gbf_solve_eo2ne_cg)
+    def _solve_eo2ne_cg(self, dst, src, eps, maxiter, graph_iterations=0, profile=0):
+        p = _lib.gbf_cg_params(float(eps), int(maxiter), int(graph_iterations), int(profile))
+        r = _lib.gbf_cg_result()
+        _lib.check(_lib.load().gbf_solve_eo2ne_cg(self.obj, src.ptr, dst.ptr, ctypes.byref(p), ctypes.byref(r), core.stream_ptr()))
+        return r
+
+
+class _even_odd_sites:
+    """base.py:288-306: DD = Mooee|D, CC = Mooee|C, CD/DC = Meooe."""
+
+    def __init__(self, op, parity):
+        self.op = op
+        self.D = parity
+        self.C = parity.inv()
+        self.DD = op.Mooee
+        self.CC = op.Mooee
+        self.CD = op.Meooe
+        self.DC = op.Meooe
+
+
+def _std_params(params, kw):
+    p = dict(params or {})
+    p.update(kw)
+    return p
+
+
+def wilson_clover(U, params=None, **kw):
+    """g.qcd.fermion.wilson_clover (lib/gpt/qcd/fermion/wilson.py:63-96)."""
+    p = _std_params(params, kw)
+    p = _copy.deepcopy(p)
+    if p.get("kappa") is not None:
+        assert p.get("mass") is None
+        p["mass"] = 1.0 / p["kappa"] / 2.0 - 4.0
+        del p["kappa"]
+    p.setdefault("csw_r", 0.0)
+    p.setdefault("csw_t", 0.0)
+    p.setdefault("cF", 1)
+    p.setdefault("n_rhs", 1)
+    bp = p.get("boundary_phases")
+    if bp is None:
+        raise ValueError("boundary_phases required")
+    if bp[-1] == 0.0:
+        raise NotImplementedError("open boundary conditions are not implemented on this path")
+    if p.get("cF", 1) != 1.0:
+        raise ValueError("cF only with open boundaries (wilson.py:89-90)")
+    return wilson_clover_operator(U, p)
+
+
+class wilson_clover_operator(fermion_operator):
+    def __init__(self, U, params, precision=None, daggered=False):
+        super().__init__("wilson_clover", U, params, precision, daggered)
+
+
+def mobius(U, params=None, **kw):
+    """g.qcd.fermion.mobius (lib/gpt/qcd/fermion/mobius.py:25-46, 325-327)."""
+    p = _std_params(params, kw)
+    if p.get("mass") is not None:
+        p["mass_plus"] = p["mass"]
+        p["mass_minus"] = p["mass"]
+    if "omega" in p:
+        raise NotImplementedError("zmobius (omega) is not implemented on this path")
+    p.setdefault("n_rhs", 1)
+    return mobius_operator(U, p)
+
+
+class mobius_operator(fermion_operator):
+    def __init__(self, U, params, precision=None, daggered=False):
+        super().__init__("mobius", U, params, precision, daggered)
+
+
+# ---------------------------------------------------------------------------
+# preconditioners (lib/gpt/qcd/fermion/preconditioner/even_odd_sites.py:61-72)
+# ---------------------------------------------------------------------------
+class preconditioner:
+    class eo2_ne:
+        """normal_equation(schur_complement_two(op, even_odd_sites_decomposed(parity)))."""
+
+        def __init__(self, params=None, parity=None):
+            par = (params or {}).get("parity", parity) if params else parity
+            self.parity = par if par is not None else core.odd
+            if self.parity is not core.odd:
+                raise NotImplementedError("eo2_ne is implemented for parity = odd (the reference default)")
+
+        def __call__(self, op):
+            return _eo2_ne_matrix(op, self.parity)
+
+
+class _eo2_ne_matrix:
+    def __init__(self, op, parity):
+        self.op = op
+        self.parity = parity

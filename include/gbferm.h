@@ -1,0 +1,155 @@
+/*
+ * gbferm.h -- C ABI of the GB300 fermion-matrix library (libgbferm.so).
+ *
+ * This is the drop-in boundary for gpt's fermion hot path.  The reference
+ * reaches Grid through the cgpt CPython functions of
+ * lib/cgpt/lib/operators.cc:34-133 (create / update / set_mass / delete /
+ * apply_fermion_operator) with the opcode numbers generated from
+ * lib/cgpt/lib/operators/types.h:26-65; the entry points below take their
+ * place, with plain pointers and sizes instead of Python objects.
+ *
+ * Conventions
+ *  - All field pointers are DEVICE pointers in the library's internal layout
+ *    unless a function says otherwise.  A half (checkerboard) field holds
+ *    N = V/2 * Ls * n_rhs "5D sites"; its size is gbf_field_bytes(op, 0).
+ *    A full field is [even half][odd half].
+ *  - "natural" layout (host interface, as in gpt's numpy views):
+ *    complex128 [V][Ls][4 spin][3 colour], site = x0 + L0*(x1 + L1*(x2 + L2*x3));
+ *    the gauge field is complex128 [4][V][3][3].
+ *  - Every call returns 0 on success or a positive error class
+ *    (GBF_E_*); gbf_last_error() gives the message of the calling thread.
+ *    No exception crosses this boundary.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    stream-ordered; functions that return host values synchronise the stream.
+ *  - Distinct operators may be used from distinct threads concurrently; one
+ *    operator must not be used by two threads at once.
+ */
+#ifndef GBFERM_H
+#define GBFERM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbf_op gbf_op;
+
+/* precision (cgpt: "single" / "double", operators.cc:36-57) */
+enum { GBF_DOUBLE = 0, GBF_SINGLE = 1, GBF_HALF = 2 };
+/* checkerboards (lib/gpt/core/checkerboard.py:22-25) */
+enum { GBF_EVEN = 0, GBF_ODD = 1, GBF_FULL = 2 };
+/* error classes */
+enum { GBF_OK = 0, GBF_E_ARG = 1, GBF_E_OOM = 2, GBF_E_CUDA = 3, GBF_E_NOCONV = 4, GBF_E_UNSUPPORTED = 5 };
+
+/* opcodes: same numbers as lib/cgpt/lib/operators/types.h via lib/gpt/qcd/fermion/register.py */
+enum {
+  GBF_M = 2001, GBF_MDAG = 2002, GBF_MEOOE = 2003, GBF_MEOOE_DAG = 2004,
+  GBF_MOOEE = 2005, GBF_MOOEE_DAG = 2006, GBF_MOOEE_INV = 2007, GBF_MOOEE_INV_DAG = 2008,
+  GBF_MDIAG = 2009, GBF_DMINUS = 2010, GBF_DMINUS_DAG = 2011,
+  GBF_IMPORT_PHYSICAL_FERMION_SOURCE = 2012, GBF_EXPORT_PHYSICAL_FERMION_SOLUTION = 2014,
+  GBF_DHOP = 3001, GBF_DHOP_EO = 3002, GBF_DHOP_DAG = 4001, GBF_DHOP_EO_DAG = 4002
+};
+
+/* Operator parameters: the keys of the reference's params dict
+ * (lib/cgpt/lib/operators/wilson_clover.h:28-39, mobius.h:42-51). */
+typedef struct {
+  int dims[4];                /* L0..L3, L0 even */
+  int Ls;                     /* mobius 5th dimension; 1 for wilson_clover */
+  int n_rhs;                  /* right-hand sides packed into one field (1..16) */
+  double mass;                /* wilson_clover m0 (kappa converted by the caller) */
+  double csw_r, csw_t, xi_0, nu;
+  int isAnisotropic;
+  double boundary_phases[8];  /* 4 complex numbers (re, im) */
+  double mass_plus, mass_minus, b, c, M5;
+  int reconstruct;            /* -1 auto, 0: 18 reals per link, 1: 12 reals (SU(3), FP32/FP16) */
+} gbf_params;
+
+/* cgpt create_fermion_operator (operators.cc:34-57): name is "wilson_clover"
+ * or "mobius".  Allocates device storage; the gauge field is set by
+ * gbf_update_gauge before first use. */
+int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op** out);
+
+/* cgpt update_fermion_operator (operators.cc:59-72): import the gauge field,
+ * natural layout complex128 [4][V][3][3], host (on_device = 0) or device
+ * memory.  Builds links, the clover term and its inverse on the device. */
+int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream);
+
+/* cgpt set_mass_fermion_operator (operators.cc:74-83). */
+int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus);
+
+/* cgpt delete_fermion_operator (operators.cc:85-94). */
+int gbf_delete(gbf_op* op);
+
+/* cgpt apply_fermion_operator (operators.cc:96-107, unary.h:20-48): apply
+ * `opcode` to n fields.  Even-odd opcodes (Meooe, Mooee, MooeeInv, DhopEO and
+ * daggers) take half fields of checkerboard src_parity (Meooe/DhopEO write
+ * the other parity); all others take full fields.  Import/Export take a 4D
+ * field (Ls = 1 layout) on one side. */
+int gbf_apply(gbf_op* op, int opcode, const void* const* src, void* const* dst, int n, int src_parity, void* stream);
+
+/* Size in bytes of a field: which = 0 half field, 1 full field, 2 full 4D
+ * field of a mobius operator (import source / export solution). */
+int gbf_field_bytes(const gbf_op* op, int which, size_t* bytes);
+
+/* Natural <-> internal transfer of one right-hand side.  `natural` is a
+ * DEVICE pointer to complex128 [V][Ls'][12] with Ls' = Ls (five_d = 1) or 1. */
+int gbf_field_import(gbf_op* op, const void* natural, void* full, int rhs, int five_d, void* stream);
+int gbf_field_export(gbf_op* op, const void* full, void* natural, int rhs, int five_d, void* stream);
+
+/* Vector algebra on internal fields of this operator's layout
+ * (lib/gpt/core/transform.py:101-153 -> cgpt transform.cc:143-247).
+ * nhalves = 1 (half field) or 2 (full field); results per rhs, accumulated in
+ * double precision with a fixed summation order (bitwise reproducible). */
+int gbf_norm2(gbf_op* op, const void* x, int nhalves, double* out, void* stream);
+int gbf_inner(gbf_op* op, const void* x, const void* y, int nhalves, double* out_re, double* out_im, void* stream);
+/* out = a*x + b*y per rhs (a complex as a_re/a_im, b real; y may be NULL) */
+int gbf_axpby(gbf_op* op, void* out, const double* a_re, const double* a_im, const void* x, const double* b, const void* y,
+              int nhalves, void* stream);
+/* dst = scale * src between two operators' layouts (same geometry), the
+ * precision change of mixed-precision solvers (cgpt transform.cc:128-141). */
+int gbf_convert(gbf_op* dst_op, void* dst, gbf_op* src_op, const void* src, double scale, int nhalves, void* stream);
+
+/* preconditioned(eo2_ne(), cg(eps, maxiter)) on device
+ * (lib/gpt/algorithms/inverter/preconditioned.py:32-54, cg.py:47-105,
+ * lib/gpt/qcd/fermion/preconditioner/even_odd_sites.py:61-72): solves
+ * M x = src for all packed right-hand sides with zero initial guess.  The CG
+ * loop runs in CUDA graphs with device-resident scalars; the host checks
+ * convergence once per graph launch. */
+typedef struct {
+  double eps;
+  int maxiter;
+  int iterations_per_graph; /* 0: default */
+  int profile;              /* 1: no graphs; CUDA events time every kernel class (diagnostic run) */
+} gbf_cg_params;
+typedef struct {
+  int iterations;
+  int converged;            /* all right-hand sides reached |r|^2 <= eps^2 |b|^2 */
+  int breakdown;            /* <p, A p> <= 0 or non-finite */
+  double residual_sq[16];   /* final |r|^2 / |b|^2 of the eo2_ne system, per rhs */
+  /* profile = 1 only: summed CUDA-event time (ms) and launch count per kernel
+   * class inside the CG loop: [0] hopping kernel, [1] site-local kernel,
+   * [2] CG update kernel */
+  double kernel_ms[3];
+  int kernel_launches[3];
+} gbf_cg_result;
+int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* p, gbf_cg_result* res, void* stream);
+
+/* Thread-local message of the last error (exception.h:21-39 analogue). */
+const char* gbf_last_error(void);
+
+/* Device synchronisation helper for callers without a CUDA runtime binding. */
+int gbf_stream_sync(void* stream);
+
+/* Number of kernels this library has launched in the process so far
+ * (a graph launch counts every kernel node it runs). */
+unsigned long long gbf_launch_count(void);
+
+/* Bytes per stored gauge link chosen by gbf_update_gauge: 144 (FP64, 18
+ * reals), 72 (FP32, 18 reals) or 48 (FP32, 12 reals, SU(3) links). */
+int gbf_link_bytes(const gbf_op* op);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFERM_H */

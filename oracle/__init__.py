@@ -77,6 +77,7 @@ def lib():
         L.orc_op_apply.argtypes = [P, I, P, P, I]
         L.orc_mobius_import.argtypes = [P, P, P, I]
         L.orc_eo2ne_cg.argtypes = [P, P, P, D, I, P]
+        L.orc_eo2ne_cg_single.argtypes = [P, P, P, D, I, P]
         L.orc_defect_correcting.argtypes = [P, P, P, D, I, D, I, P, P]
         L.orc_num_threads.restype = I
         _lib = L
@@ -251,6 +252,16 @@ class _op:
         x = np.zeros(self.shape(), dtype=np.complex128)
         res = np.zeros(1)
         it = lib().orc_eo2ne_cg(self.obj, _ptr(src), _ptr(x), eps, maxiter, _ptr(res))
+        if it <= -1000000000:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return x, it, float(res[0])
+
+    def eo2ne_cg_single(self, src, eps, maxiter):
+        """The same solve with the single-precision operator (needs with_single=True)."""
+        src = np.ascontiguousarray(src, dtype=np.complex128)
+        x = np.zeros(self.shape(), dtype=np.complex128)
+        res = np.zeros(1)
+        it = lib().orc_eo2ne_cg_single(self.obj, _ptr(src), _ptr(x), eps, maxiter, _ptr(res))
         if it <= -1000000000:
             raise RuntimeError(lib().orc_last_error().decode())
         return x, it, float(res[0])

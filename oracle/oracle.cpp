@@ -768,6 +768,8 @@ struct OpBase {
   int n5 = 1;  // 5th-dimension entries per 4D site
   virtual ~OpBase() {}
   virtual void Meooe(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const = 0;
+  // the hopping term alone (Grid's Dhop/DhopEO: for the 5D operator the 4D hop on every s-slice)
+  virtual void Dhop(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const = 0;
   virtual void Mooee(cx<T>* out, const cx<T>* in, int parity, bool dag, bool inv) const = 0;
   size_t site_len() const { return (size_t)n5 * 12; }
 };
@@ -845,6 +847,7 @@ struct WilsonClover : OpBase<T> {
     if (!ok) throw std::runtime_error("singular clover block");
   }
   void Meooe(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const override { hop.apply(out, in, out_parity, dag, 1); }
+  void Dhop(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const override { hop.apply(out, in, out_parity, dag, 1); }
   void Mooee(cx<T>* out, const cx<T>* in, int parity, bool dag, bool inv) const override {
     const long V = G->V;
     const std::vector<int32_t>* list = parity < 2 ? &G->par_sites[parity] : nullptr;
@@ -940,6 +943,7 @@ struct Mobius : OpBase<T> {
       }
     }
   }
+  void Dhop(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const override { hop.apply(out, in, out_parity, dag, Ls); }
   void Meooe(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const override {
     // out = Dhop B in  (dag: B^+ Dhop^+ in); B acts on the source parity
     size_t len = (size_t)G->V * Ls * 12;
@@ -1150,8 +1154,8 @@ static void apply_full(const OpBase<T>* op, int opcode, cx<T>* out, const cx<T>*
     case OP_MOOEE_INV: op->Mooee(out, in, parity, false, true); break;
     case OP_MOOEE_INV_DAG: op->Mooee(out, in, parity, true, true); break;
     case OP_MDIAG: op->Mooee(out, in, 2, false, false); break;
-    case OP_DHOP: op->Meooe(out, in, 2, false); break;
-    case OP_DHOP_DAG: op->Meooe(out, in, 2, true); break;
+    case OP_DHOP: op->Dhop(out, in, 2, false); break;
+    case OP_DHOP_DAG: op->Dhop(out, in, 2, true); break;
     default: throw std::runtime_error("opcode not supported by this operator");
   }
 }
@@ -1282,6 +1286,23 @@ int orc_eo2ne_cg(void* o, const double* src, double* x, double eps, int maxiter,
   try {
     OracleOp& op = *(OracleOp*)o;
     return eo2ne_solve<double>(op.d.get(), reinterpret_cast<cd*>(x), reinterpret_cast<const cd*>(src), eps, maxiter, res);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1000000000;
+  }
+}
+
+// eo2_ne CG of the single-precision operator (inner solve of the mixed method).
+int orc_eo2ne_cg_single(void* o, const double* src, double* x, double eps, int maxiter, double* res) {
+  try {
+    OracleOp& op = *(OracleOp*)o;
+    if (!op.f) throw std::runtime_error("single-precision operator not built");
+    size_t len = (size_t)op.G->V * op.d->site_len();
+    std::vector<cx<float>> sf(len), xf(len, cx<float>{0, 0});
+    for (size_t k = 0; k < len; ++k) sf[k] = {(float)src[2 * k], (float)src[2 * k + 1]};
+    int it = eo2ne_solve<float>(op.f.get(), xf.data(), sf.data(), eps, maxiter, res);
+    for (size_t k = 0; k < len; ++k) { x[2 * k] = xf[k].re; x[2 * k + 1] = xf[k].im; }
+    return it;
   } catch (const std::exception& e) {
     g_err = e.what();
     return -1000000000;
