@@ -50,7 +50,36 @@ def parse():
     ap.add_argument("--dims", type=str, default=None, help="override lattice, e.g. 16,16,16,16 (tests only)")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-dslash", action="store_true",
+                    help="profiling case: FP32 operator only, one inner eo2_ne CG of 12 iterations")
     return ap.parse_args()
+
+
+def run_profile_case(args, dims):
+    """A small-footprint run of the inner FP32 solve (about 1.5 GB on the
+    device at 32^4) for ncu captures of the hopping kernel."""
+    import torch
+
+    import gpt_gb300 as g
+
+    g.load()
+    grid = g.grid(dims, g.double)
+    U = g.qcd.gauge.random_su3(grid, CFG["gauge_eps"], CFG["gauge_seed"])
+    params = dict(mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"], boundary_phases=CFG["phases"])
+    op = g.qcd.fermion.wilson_clover_operator(U, params, precision=g.single)
+    V = grid.gsites
+    rng = np.random.default_rng(CFG["src_seed"])
+    src = op.F_lattice()
+    src[:] = (rng.standard_normal((V, 4, 3)) + 1j * rng.standard_normal((V, 4, 3))) * 1e-3
+    x = op.F_lattice()
+    for _ in range(args.warmup):
+        op._solve_eo2ne_cg(x, src, 1e-30, 12)
+    torch.cuda.synchronize()
+    r = op._solve_eo2ne_cg(x, src, 1e-30, 12)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "wilson_clover FP32 eo2_ne CG, 12 iterations", "lattice": dims,
+                      "iterations": r.iterations, "link_bytes": op.link_bytes()}))
+    return 0
 
 
 def workload_config(dims):
@@ -405,6 +434,8 @@ def run_gbf(args, dims):
 def main():
     args = parse()
     dims = [int(d) for d in args.dims.split(",")] if args.dims else CFG["dims"]
+    if args.profile_dslash:
+        return run_profile_case(args, dims)
     if args.impl == "reference":
         return run_reference(args, dims)
     return run_gbf(args, dims)

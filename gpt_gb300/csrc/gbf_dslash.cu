@@ -18,11 +18,16 @@
 // pipe on GB300 (about 1.2 TFLOP/s measured).
 #include "gbf_launch.cuh"
 
+// resident blocks of 256 threads per SM requested for the FP32/FP16 variants
+// (register cap 65536 / (256 * minblocks))
+#ifndef GBF_DSLASH_MINB
+#define GBF_DSLASH_MINB 2
+#endif
+
 namespace gbf {
 
-
 template <int P, int LS, int LK>
-__global__ void __launch_bounds__(256) dslash_kernel(const DslashArgs a) {
+__global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_kernel(const DslashArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
   extern __shared__ double smem_d[];
@@ -130,14 +135,9 @@ __global__ void __launch_bounds__(256) dslash_kernel(const DslashArgs a) {
       if (a.red == 1) {
         V yv[12];
         load_spinor<P>(a.Y, g.N, n, yv);
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-          vr += (double)yv[k].x * res[k].x + (double)yv[k].y * res[k].y;
-          vi += (double)yv[k].x * res[k].y - (double)yv[k].y * res[k].x;
-        }
+        site_dot<R>(yv, res, vr, vi);
       } else {
-#pragma unroll
-        for (int k = 0; k < 12; ++k) vr += (double)res[k].x * res[k].x + (double)res[k].y * res[k].y;
+        vr = site_norm2<R>(res);
       }
     }
     double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);

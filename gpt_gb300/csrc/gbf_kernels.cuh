@@ -117,6 +117,33 @@ __device__ __forceinline__ void smat_apply_block(const R* mat_g, int Ls, R* tile
   __syncthreads();
 }
 
+// Per-site <a, b> and |a|^2: the 12 products of one site are summed in the
+// arithmetic precision R (FP32 kernels stay on the FP32 pipe; FP64 throughput
+// is 1/58 of FP32 on GB300), the cross-site sums below are FP64.
+template <typename R>
+__device__ __forceinline__ void site_dot(const cplx<R> (&a)[12], const cplx<R> (&b)[12], double& re, double& im) {
+  R r = 0, i = 0;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    r = fma(a[k].x, b[k].x, r);
+    r = fma(a[k].y, b[k].y, r);
+    i = fma(a[k].x, b[k].y, i);
+    i = fma(-a[k].y, b[k].x, i);
+  }
+  re = (double)r;
+  im = (double)i;
+}
+template <typename R>
+__device__ __forceinline__ double site_norm2(const cplx<R> (&a)[12]) {
+  R r = 0;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    r = fma(a[k].x, a[k].x, r);
+    r = fma(a[k].y, a[k].y, r);
+  }
+  return (double)r;
+}
+
 // ---------------------------------------------------------------------------
 // deterministic reduction: block tree over sites (stride N5), per-rhs sum of
 // the s entries, per-block partials, last block sums the partials in block

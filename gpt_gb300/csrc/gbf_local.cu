@@ -68,14 +68,9 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
       if (a.red == 1) {
         V yv[12];
         load_spinor<P>(a.Y, g.N, n, yv);
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-          vr += (double)yv[k].x * v[k].x + (double)yv[k].y * v[k].y;
-          vi += (double)yv[k].x * v[k].y - (double)yv[k].y * v[k].x;
-        }
+        site_dot<R>(yv, v, vr, vi);
       } else {
-#pragma unroll
-        for (int k = 0; k < 12; ++k) vr += (double)v[k].x * v[k].x + (double)v[k].y * v[k].y;
+        vr = site_norm2<R>(v);
       }
     }
     double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
@@ -139,8 +134,8 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
     for (int k = 0; k < 12; ++k) {
       r[k] = mk<R>(fma(-al, m[k].x, r[k].x), fma(-al, m[k].y, r[k].y));
       x[k] = mk<R>(fma(al, p[k].x, x[k].x), fma(al, p[k].y, x[k].y));
-      vr += (double)r[k].x * r[k].x + (double)r[k].y * r[k].y;
     }
+    vr = site_norm2<R>(r);
     store_spinor<P>(a.r, g.N, n, r);
     store_spinor<P>(a.x, g.N, n, x);
   }
@@ -180,11 +175,7 @@ __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
 #pragma unroll
       for (int k = 0; k < 12; ++k) y[k] = cz<R>();
     if (a.red == 3) {
-#pragma unroll
-      for (int k = 0; k < 12; ++k) {
-        vr += (double)x[k].x * y[k].x + (double)x[k].y * y[k].y;
-        vi += (double)x[k].x * y[k].y - (double)x[k].y * y[k].x;
-      }
+      site_dot<R>(x, y, vr, vi);
     } else {
       const V ac = mk<R>((R)a.a_re[rhs], (R)a.a_im[rhs]);
       const R bc = (R)a.b_re[rhs];
@@ -194,9 +185,7 @@ __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
         o[k] = mk<R>(fma(bc, y[k].x, t.x), fma(bc, y[k].y, t.y));
       }
       if (a.write) store_spinor<P>(a.out, g.N, n, o);
-      if (a.red == 2)
-#pragma unroll
-        for (int k = 0; k < 12; ++k) vr += (double)o[k].x * o[k].x + (double)o[k].y * o[k].y;
+      if (a.red == 2) vr = site_norm2<R>(o);
     }
   }
   if (a.red) block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, smem_d);
