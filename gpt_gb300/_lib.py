@@ -97,6 +97,8 @@ def load():
         "gbf_stream_sync": (I, [P]),
         "gbf_launch_count": (ctypes.c_ulonglong, []),
         "gbf_link_bytes": (I, [P]),
+        "gbf_norm2_noalloc": (I, [I, P, ctypes.c_longlong, I, DP, P]),
+        "gbf_norm2_noalloc_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -149,6 +149,22 @@ unsigned long long gbf_launch_count(void);
  * reals), 72 (FP32, 18 reals) or 48 (FP32, 12 reals, SU(3) links). */
 int gbf_link_bytes(const gbf_op* op);
 
+/* |x|^2 of a field, allocating nothing (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc: a process whose free HBM belongs
+ * to its own pool, or a latency-critical loop that must not take cudaMalloc's
+ * device-wide synchronisation (gbf_norm2 allocates its workspace on first
+ * use).  x: device field of `precision` with n_sites 5D sites per half and
+ * nhalves halves (the layout of gbf_field_bytes); the sum over all sites is
+ * written to the host double *out after the stream is synchronised.
+ * The reduction scratch is a static device array of about 263 KB, reserved on
+ * every GPU that loads the library until the process exits; at most
+ * 4194304 sites per half (larger sizes return GBF_E_ARG).  The first call on
+ * a device sets the array's address up for that device (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race.  Errors: gbf_norm2_noalloc_error(). */
+int gbf_norm2_noalloc(int precision, const void* x, long long n_sites, int nhalves, double* out, void* stream);
+const char* gbf_norm2_noalloc_error(void);
+
 #ifdef __cplusplus
 }
 #endif
