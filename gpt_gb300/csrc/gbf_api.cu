@@ -336,8 +336,6 @@ void read_last(gbf_op* op, cudaStream_t s, double* re, double* im) {
   }
 }
 
-const Geo& geo_for(gbf_op* op, int nhalves_4d) { return nhalves_4d ? op->g4 : op->g; }
-
 }  // namespace
 
 // ===========================================================================
