@@ -117,9 +117,14 @@ class defect_correcting:
             s = src.new()
             t = src.new()
             me.history = []
+            psi_zero = core.norm2(psi)
+            psi_zero = all(v == 0.0 for v in ([psi_zero] if n == 1 else psi_zero))
             for i in range(me.maxiter):
-                outer_mat(t, psi)
-                core.axpby(s, -1.0, t, 1.0, src)
+                if i == 0 and psi_zero:
+                    core.copy(s, src)  # src - M * 0, without applying M
+                else:
+                    outer_mat(t, psi)
+                    core.axpby(s, -1.0, t, 1.0, src)
                 nd = core.norm2(s)
                 nd = [nd] if n == 1 else nd
                 eps = max(math.sqrt(nd[j] / ns[j]) for j in range(n))

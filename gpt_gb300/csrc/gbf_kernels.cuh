@@ -200,27 +200,61 @@ __device__ __forceinline__ void finalize(const RedArgs& r, int rhs, double re, d
   }
 }
 
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum (a, b) over the block in a fixed order: shuffle within warps, then the
+// warp sums in warp 0.  Needs blockDim % 32 == 0; result valid in thread 0.
+__device__ __forceinline__ double2 block_sum_shfl(double a, double b, double* sm) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) {
+    sm[w] = a;
+    sm[32 + w] = b;
+  }
+  __syncthreads();
+  if (w == 0) {
+    a = lane < nw ? sm[lane] : 0.0;
+    b = lane < nw ? sm[32 + lane] : 0.0;
+    a = warp_sum(a);
+    b = warp_sum(b);
+  }
+  __syncthreads();
+  return make_double2(a, b);
+}
+
 // sm: 2*blockDim doubles of shared memory.  Every thread of the block calls.
 __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double vre, double vim, int N5, int Ls, int nrhs, double* sm) {
   const int t = threadIdx.x, bd = blockDim.x;
-  const int S = bd / N5;  // power of two by construction
-  sm[t] = vre;
-  sm[bd + t] = vim;
-  __syncthreads();
-  for (int k = S >> 1; k >= 1; k >>= 1) {
-    if (t < k * N5) {
-      sm[t] += sm[t + k * N5];
-      sm[bd + t] += sm[bd + t + k * N5];
-    }
+  const bool shfl = (bd & 31) == 0;
+  if (nrhs == 1 && shfl) {
+    // one right-hand side: every thread's value belongs to it
+    const double2 s = block_sum_shfl(vre, vim, sm);
+    if (t == 0) r.partial[blockIdx.x] = s;
+  } else {
+    const int S = bd / N5;  // power of two by construction
+    sm[t] = vre;
+    sm[bd + t] = vim;
     __syncthreads();
-  }
-  if (t < nrhs) {
-    double ar = 0, ai = 0;
-    for (int s = 0; s < Ls; ++s) {
-      ar += sm[t * Ls + s];
-      ai += sm[bd + t * Ls + s];
+    for (int k = S >> 1; k >= 1; k >>= 1) {
+      if (t < k * N5) {
+        sm[t] += sm[t + k * N5];
+        sm[bd + t] += sm[bd + t + k * N5];
+      }
+      __syncthreads();
     }
-    r.partial[(size_t)blockIdx.x * nrhs + t] = make_double2(ar, ai);
+    if (t < nrhs) {
+      double ar = 0, ai = 0;
+      for (int s = 0; s < Ls; ++s) {
+        ar += sm[t * Ls + s];
+        ai += sm[bd + t * Ls + s];
+      }
+      r.partial[(size_t)blockIdx.x * nrhs + t] = make_double2(ar, ai);
+    }
   }
   __threadfence();
   __syncthreads();
@@ -237,6 +271,12 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double v
       double2 q = __ldcg(r.partial + (size_t)b * nrhs + rhs);
       ar += q.x;
       ai += q.y;
+    }
+    if (shfl) {
+      const double2 s = block_sum_shfl(ar, ai, sm);
+      if (t == 0) finalize(r, rhs, s.x, s.y);
+      __syncthreads();
+      continue;
     }
     sm[t] = ar;
     sm[bd + t] = ai;
