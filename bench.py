@@ -52,7 +52,253 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-dslash", action="store_true",
                     help="profiling case: FP32 operator only, one inner eo2_ne CG of 12 iterations")
+    ap.add_argument("--profile-mobius", action="store_true",
+                    help="profiling case: FP32 mobius 12^3x24 Ls 12 with 12 packed rhs, 12 CG iterations")
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2 (default): wilson_clover 32^4 mixed vs plain; c1: wilson_clover 8^4; c3: mobius "
+                         "16^3x32 Ls=12, 12 point sources; c4: mobius 32^3x64 Ls=16, 12 sources; c5: serving stream")
+    ap.add_argument("--requests", type=int, default=40, help="c5: number of requests")
+    ap.add_argument("--inner", default="single", choices=["single", "half"], help="c3/c4 inner precision")
+    ap.add_argument("--rhs-group", type=int, default=0, help="c4: right-hand sides solved together (0: auto)")
     return ap.parse_args()
+
+
+def run_profile_mobius(args):
+    """Profiling case of the 5D multi-rhs path (about 4 GB on the device)."""
+    import torch
+
+    import gpt_gb300 as g
+
+    g.load()
+    dims = [12, 12, 12, 24]
+    grid = g.grid(dims, g.double)
+    U = g.qcd.gauge.random_su3_device(grid, 0.4, 4242)
+    params = dict(Ls=12, b=1.5, c=0.5, M5=1.8, mass_plus=0.01, mass_minus=0.01, boundary_phases=[1.0, 1.0, 1.0, -1.0],
+                  n_rhs=12)
+    op = g.qcd.fermion.mobius_operator(U, params, precision=g.single)
+    src = op.F_lattice()
+    L = g._lib.load()
+    V = grid.gsites
+    nat = torch.empty(V * 12 * 24, dtype=torch.float64, device="cuda")
+    for k in range(12):
+        g._lib.check(L.gbf_random_spinor(V * 12 * 12, 50 + k, nat.data_ptr(), g.core.stream_ptr()))
+        g._lib.check(L.gbf_field_import(src.layout.op, nat.data_ptr(), src.ptr, k, 1, g.core.stream_ptr()))
+    x = op.F_lattice()
+    for _ in range(args.warmup):
+        op._solve_eo2ne_cg(x, src, 1e-30, 12)
+    r = op._solve_eo2ne_cg(x, src, 1e-30, 12, 0, 1)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "mobius FP32 12^3x24 Ls 12, 12 rhs, eo2_ne CG 12 iterations", "iterations": r.iterations,
+                      "kernel_ms": list(r.kernel_ms), "kernel_launches": list(r.kernel_launches)}))
+    return 0
+
+
+def _common_line(metric, value, unit, args, world, total_ms, dims_cfg, dtype, extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": dims_cfg}
+    line.update(extra)
+    return line
+
+
+def run_mobius_config(args, which):
+    """c3: Mobius 16^3x32, Ls 12, b 1.5, c 0.5, M5 1.8, mass 0.01, gauge eps 0.4,
+    12 point sources (every spin-colour component at site 0) as one packed
+    12-rhs field, propagator = Export * solve * Import, to true residual 1e-8.
+    c4: Mobius 32^3x64, Ls 16, mass 0.005, 12 Gaussian sources, to 1e-10,
+    solved in groups of right-hand sides that fit HBM."""
+    import torch
+
+    import gpt_gb300 as g
+
+    L = g.load()
+    if which == "c3":
+        dims, Ls, mass, geps, tol, nsrc = [16, 16, 16, 32], 12, 0.01, 0.4, 1e-8, 12
+        group = 12
+    else:
+        dims, Ls, mass, geps, tol, nsrc = [32, 32, 32, 64], 16, 0.005, 0.4, 1e-10, 12
+        group = args.rhs_group or 2
+    grid = g.grid(dims, g.double)
+    U = g.qcd.gauge.random_su3_device(grid, geps, 4242)
+    inner_prec = g.half if args.inner == "half" else g.single
+    inner_tol = 1e-5 if args.inner == "single" else 3e-3
+    V = grid.gsites
+    ngroups = (nsrc + group - 1) // group
+    params = dict(Ls=Ls, b=1.5, c=0.5, M5=1.8, mass=mass, boundary_phases=[1.0, 1.0, 1.0, -1.0], n_rhs=group)
+    op = g.qcd.fermion.mobius(U, params)
+    inv = g.algorithms.inverter
+    pc = g.qcd.fermion.preconditioner
+    inner_cg = inv.cg({"eps": inner_tol, "maxiter": 50000, "iterations_per_graph": 16})
+    dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inner_cg), inner_prec, g.double),
+                               eps=tol, maxiter=200)
+    solver = dc(op)
+    last5 = {}
+
+    def prop(s4):
+        # propagator = Export * solver * Import (operator/base.py:270-286)
+        b5 = op.ImportPhysicalFermionSource(s4)
+        x5 = solver(b5)
+        last5.clear()  # keep only the latest group's 5D fields (HBM)
+        last5[id(s4)] = (b5, x5)
+        return op.ExportPhysicalFermionSolution(x5)
+
+    srcs = []
+    for grp in range(ngroups):
+        s4 = op.U_lattice()
+        nat = torch.zeros(V * 24, dtype=torch.float64, device="cuda")
+        for k in range(group):
+            kk = grp * group + k
+            if which == "c3":
+                nat.zero_()
+                nat[2 * kk] = 1.0  # site 0, spin-colour component kk (real part)
+            else:
+                g._lib.check(L.gbf_random_spinor(V * 12, 1000 + kk, nat.data_ptr(), g.core.stream_ptr()))
+            g._lib.check(L.gbf_field_import(s4.layout.op, nat.data_ptr(), s4.ptr, k, 0, g.core.stream_ptr()))
+        srcs.append(s4)
+    stream = torch.cuda.current_stream()
+
+    def one_step():
+        outs = []
+        for s4 in srcs:
+            outs.append(prop(s4))
+        return outs
+
+    for _ in range(args.warmup):
+        one_step()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    torch.cuda.synchronize()
+    n0 = L.gbf_launch_count()
+    before = inner_cg.total_iterations
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        outs = one_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    n1 = L.gbf_launch_count()
+    clk = clocks.stop()
+    total_ms = e0.elapsed_time(e1)
+    inner_its = (inner_cg.total_iterations - before) // max(1, args.steps)
+    # true residual of the 5D systems of the last step, FP64
+    worst = 0.0
+    for b5, x5 in last5.values():  # the last group solved
+        r5 = op.F_lattice()
+        op.M(r5, x5)
+        g.axpby(r5, -1.0, r5, 1.0, b5)
+        nr, nb = g.norm2(r5), g.norm2(b5)
+        nr, nb = ([nr], [nb]) if group == 1 else (nr, nb)
+        worst = max(worst, max(math.sqrt(a / b) for a, b in zip(nr, nb)))
+    value = nsrc * args.steps / (total_ms / 1000.0)
+    cfg = {"workload": f"mobius {'x'.join(map(str, dims))} Ls {Ls} b 1.5 c 0.5 M5 1.8 mass {mass} gauge eps {geps}, "
+                       f"{nsrc} {'point' if which == 'c3' else 'gaussian'} sources in {ngroups} packed group(s) of {group}, "
+                       f"propagator Export*solve*Import, defect correction ({args.inner} inner, tol {inner_tol}) "
+                       f"to true residual {tol}", "lattice": dims, "Ls": Ls,
+           "l2_policy": "inputs larger than L2; no flush", "parallelism": "replicas"}
+    line = _common_line(METRIC, value, "solves/s", args, 1, total_ms, cfg, f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",
+                        {"gpu_launches": int(n1 - n0), "clocks": clk, "true_residual_5d": worst,
+                         "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
+                         "ms_per_solve": total_ms / args.steps / nsrc})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_c1(args):
+    """c1: Wilson-clover 8^4, gauge eps 0.5, mass 0.1, csw 1.0: one Dslash (M)
+    application and the plain eo2_ne CG to 1e-10 (maxiter 1000), FP64, with
+    the oracle comparison."""
+    import torch
+
+    import gpt_gb300 as g
+    import oracle as o
+
+    L = g.load()
+    dims = [8, 8, 8, 8]
+    grid = g.grid(dims, g.double)
+    U = g.qcd.gauge.random_su3(grid, 0.5, 8)
+    p = dict(mass=0.1, csw_r=1.0, csw_t=1.0, boundary_phases=[1.0, 1.0, 1.0, -1.0])
+    op = g.qcd.fermion.wilson_clover(U, p)
+    rng = np.random.default_rng(1)
+    s = rng.standard_normal((grid.gsites, 4, 3)) + 1j * rng.standard_normal((grid.gsites, 4, 3))
+    src = op.F_lattice()
+    src[:] = s
+    inv = g.algorithms.inverter
+    pc = g.qcd.fermion.preconditioner
+    cg = inv.cg({"eps": 1e-10, "maxiter": 1000})
+    slv = inv.preconditioned(pc.eo2_ne(), cg)(op)
+    out = op.F_lattice()
+    for _ in range(args.warmup):
+        op.M(out, src)
+        slv(src)
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record(stream)
+    for _ in range(100):
+        op.M(out, src)
+    e[1].record(stream)
+    for _ in range(args.steps):
+        x = slv(src)
+    e[2].record(stream)
+    torch.cuda.synchronize()
+    m_us = e[0].elapsed_time(e[1]) * 10.0
+    total_ms = e[1].elapsed_time(e[2])
+    ref = o.wilson_clover(U.U, dims, **p)
+    m_err = float(np.linalg.norm(out[:] - ref.apply("M", s)) / np.linalg.norm(ref.apply("M", s)))
+    xr = x[:]
+    tres = float(np.sqrt(o.norm2(s - ref.apply("M", xr)) / o.norm2(s)))
+    cfg = {"workload": "wilson_clover 8^4 gauge eps 0.5 mass 0.1 csw 1.0 bc [1,1,1,-1], 1 gaussian source, "
+                       "one M application + plain FP64 eo2_ne CG to 1e-10", "lattice": dims,
+           "l2_policy": "small case: resident in L2 (reported, not a roofline number)", "parallelism": "replicas"}
+    line = _common_line(METRIC, args.steps / (total_ms / 1000.0), "solves/s", args, 1, total_ms, cfg, "f64",
+                        {"M_application_us": m_us, "M_vs_oracle_rel": m_err, "cg_iterations": cg.last.iterations,
+                         "true_residual_oracle": tres})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_c5(args):
+    """c5: Poisson stream at 20 req/s of Wilson-clover propagator requests,
+    L in {8,16,24,32}, gauge eps U[0.2,0.5], mass U[0.01,0.2], 1-12 sources,
+    true residual 1e-10, mixed method with continuous batching, against the
+    same stream solved serially with plain FP64 CG."""
+    import torch
+
+    import gpt_gb300 as g
+    from gpt_gb300 import serving
+
+    g.load()
+    reqs = serving.poisson_stream(args.requests, 20.0, seed=2026)
+    free, total = torch.cuda.mem_get_info()
+    budget = int(0.8 * free)
+    ex = serving.gpu_executor()
+    # warm-up: one small request of every size (library, graphs, allocator)
+    serving.Server(ex, budget, realtime=False).run([serving.Request(-1 - i, L, 0.3, 5, 0.1, 1, 6)
+                                                     for i, L in enumerate([8, 16, 24, 32])])
+    L = g._lib.load()
+    n0 = L.gbf_launch_count()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    res, wall = serving.Server(ex, budget, method="mixed").run(reqs)
+    clk = clocks.stop()
+    n1 = L.gbf_launch_count()
+    s = serving.summarize(res, wall)
+    serial, swall = serving.Server(ex, budget, caps={8: 1, 16: 1, 24: 1, 32: 1}, method="plain", realtime=False).run(reqs)
+    for r in serial:  # serial: one request at a time, so latency = completion - arrival of a queue drained in order
+        pass
+    ss = serving.summarize(serial, swall)
+    cfg = {"workload": f"serving: {args.requests} Poisson requests at 20/s, wilson_clover L^4 L in {{8,16,24,32}}, "
+                       "gauge eps U[0.2,0.5], mass U[0.01,0.2], 1-12 gaussian sources, true residual 1e-10; "
+                       "mixed method with HBM-footprint admission and batching by lattice size",
+           "hbm_budget_bytes": budget, "l2_policy": "per-request working sets; no flush", "parallelism": "replicas"}
+    line = _common_line(METRIC, s["solves_per_s"], "solves/s", args, 1, 1000.0 * wall, cfg, "f32 inner / f64 outer",
+                        {"p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "requests_per_s": s["requests_per_s"],
+                         "failed": s["failed"], "max_true_residual": s["max_true_residual"], "gpu_launches": int(n1 - n0),
+                         "clocks": clk, "serial_plain_fp64": {"solves_per_s": ss["solves_per_s"], "wall_s": swall,
+                                                               "max_true_residual": ss["max_true_residual"]},
+                         "speedup_vs_serial_plain": s["solves_per_s"] / ss["solves_per_s"] if ss["solves_per_s"] else None})
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def run_profile_case(args, dims):
@@ -436,6 +682,14 @@ def main():
     dims = [int(d) for d in args.dims.split(",")] if args.dims else CFG["dims"]
     if args.profile_dslash:
         return run_profile_case(args, dims)
+    if args.profile_mobius:
+        return run_profile_mobius(args)
+    if args.impl != "reference" and args.config == "c1":
+        return run_c1(args)
+    if args.impl != "reference" and args.config in ("c3", "c4"):
+        return run_mobius_config(args, args.config)
+    if args.impl != "reference" and args.config == "c5":
+        return run_c5(args)
     if args.impl == "reference":
         return run_reference(args, dims)
     return run_gbf(args, dims)

@@ -97,6 +97,8 @@ def load():
         "gbf_stream_sync": (I, [P]),
         "gbf_launch_count": (ctypes.c_ulonglong, []),
         "gbf_link_bytes": (I, [P]),
+        "gbf_random_gauge": (I, [ctypes.POINTER(ctypes.c_int), D, ctypes.c_ulonglong, P, P]),
+        "gbf_random_spinor": (I, [ctypes.c_longlong, ctypes.c_ulonglong, P, P]),
         "gbf_norm2_noalloc": (I, [I, P, ctypes.c_longlong, I, DP, P]),
         "gbf_norm2_noalloc_error": (ctypes.c_char_p, []),
     }

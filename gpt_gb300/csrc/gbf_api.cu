@@ -89,7 +89,7 @@ struct gbf_op {
   void* smat = nullptr;          // [S_COUNT][2][Ls][Ls] in the arithmetic precision
   std::vector<double> smat_host; // same in double
   // workspace
-  void* ws = nullptr;
+  void* pair_mem[6] = {};        // workspace: full fields allocated on first use
   void* tmp[12] = {};
   double2* partial = nullptr;
   unsigned* counter = nullptr;
@@ -102,6 +102,10 @@ struct gbf_op {
   int graph_K = 0;
 
   size_t half() const { return (size_t)half_bytes(prec, g.N); }
+  // workspace half field i; halves 2k and 2k+1 are one contiguous full field,
+  // allocated when first used (an operator that only applies M never holds
+  // the CG's vectors)
+  void* T(int i);
   size_t half4() const { return (size_t)half_bytes(prec, g4.N); }
   size_t rb() const { return prec == P64 ? 8 : 4; }
 
@@ -191,6 +195,17 @@ struct gbf_op {
     count_launch();
   }
 };
+
+void* gbf_op::T(int i) {
+  if (i < 0 || i >= 12) throw Fail(GBF_E_ARG, "internal: workspace index");
+  const int pr = i / 2;
+  if (!pair_mem[pr]) {
+    pair_mem[pr] = dmalloc(2 * half());
+    tmp[2 * pr] = pair_mem[pr];
+    tmp[2 * pr + 1] = (char*)pair_mem[pr] + half();
+  }
+  return tmp[i];
+}
 
 namespace {
 
@@ -290,11 +305,7 @@ void build_smat(gbf_op* op) {
 }
 
 void ensure_ws(gbf_op* op) {
-  if (op->ws) return;
-  const size_t h = op->half();
-  const int ntmp = 12;
-  op->ws = dmalloc(h * ntmp);
-  for (int i = 0; i < ntmp; ++i) op->tmp[i] = (char*)op->ws + (size_t)i * h;
+  if (op->partial) return;
   const long long maxblocks = op->g.Vh + 1;
   op->partial = (double2*)dmalloc((size_t)maxblocks * op->g.nrhs * sizeof(double2));
   op->counter = (unsigned*)dmalloc(sizeof(unsigned) * 4);
@@ -314,7 +325,7 @@ void free_op(gbf_op* op) {
   cudaFree(op->links);
   cudaFree(op->clov_mem);
   cudaFree(op->smat);
-  cudaFree(op->ws);
+  for (void* m : op->pair_mem) cudaFree(m);
   cudaFree(op->partial);
   cudaFree(op->counter);
   cudaFree(op->st);
@@ -436,7 +447,12 @@ int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream) {
     for (int k = 0; k < 8; ++k) ph[k] = op->par.boundary_phases[k];
     if (!op->links) op->links = dmalloc((size_t)8 * link_bytes_per_parity_mu(op->prec == P64 ? L64 : L32, g.Vh));
     int LS = op->prec == P64 ? L64 : L32;
-    if (op->prec != P64 && op->par.reconstruct != 0) {
+    // 12-real links save 24 B per link per output site, but cost a
+    // reconstruction and a run-time phase in every thread.  When Ls * n_rhs
+    // threads share each link (5D / multi-rhs fields) the link bytes are
+    // already amortised and those flops would dominate: keep 18 reals.
+    const bool try_r12 = op->par.reconstruct == 1 || (op->par.reconstruct != 0 && op->g.N5 < 4);
+    if (op->prec != P64 && try_r12) {
       CK(cudaMemsetAsync(op->errbits, 0, sizeof(unsigned), s));
       CK(launch_pack_links(L32R, g, Ud, op->links, lam, ph, op->errbits, s));
       unsigned eb = 0;
@@ -598,8 +614,8 @@ static void apply_one(gbf_op* op, int opcode, const void* src, void* dst, int sp
       const bool dag = opcode == GBF_MEOOE_DAG || opcode == GBF_DHOP_EO_DAG;
       const bool meo = opcode == GBF_MEOOE || opcode == GBF_MEOOE_DAG;
       if (mob && meo && !dag) {
-        op->local(s, sp, src, op->tmp[0], op->B(false));
-        op->dslash(s, 1 - sp, false, op->tmp[0], dst, op->none());
+        op->local(s, sp, src, op->T(0), op->B(false));
+        op->dslash(s, 1 - sp, false, op->T(0), dst, op->none());
       } else {
         op->dslash(s, 1 - sp, dag, src, dst, (mob && meo) ? op->B(true) : op->none());
       }
@@ -627,12 +643,12 @@ static void apply_one(gbf_op* op, int opcode, const void* src, void* dst, int sp
         if (!mob) {
           op->dslash(s, p, dag, H(src, 1 - p), HW(dst, p), op->none(), 1.0, H(src, p), 1.0, op->A(dag));
         } else {
-          op->local(s, p, H(src, p), op->tmp[1], op->A(dag));
+          op->local(s, p, H(src, p), op->T(1), op->A(dag));
           if (!dag) {
-            op->local(s, 1 - p, H(src, 1 - p), op->tmp[0], op->B(false));
-            op->dslash(s, p, false, op->tmp[0], HW(dst, p), op->none(), 1.0, op->tmp[1], 1.0);
+            op->local(s, 1 - p, H(src, 1 - p), op->T(0), op->B(false));
+            op->dslash(s, p, false, op->T(0), HW(dst, p), op->none(), 1.0, op->T(1), 1.0);
           } else {
-            op->dslash(s, p, true, H(src, 1 - p), HW(dst, p), op->B(true), 1.0, op->tmp[1], 1.0);
+            op->dslash(s, p, true, H(src, 1 - p), HW(dst, p), op->B(true), 1.0, op->T(1), 1.0);
           }
         }
       }
@@ -707,8 +723,8 @@ static constexpr int kKernelsPerIteration = 6;
 // ev (optional, profile mode): 7 events recorded around the six launches
 static void cg_iteration(gbf_op* op, cudaStream_t s, cudaEvent_t* ev = nullptr) {
   const int D = GBF_ODD, C = GBF_EVEN;
-  void *t = op->tmp[0], *z = op->tmp[1], *w = op->tmp[2], *u = op->tmp[3];
-  void *p = op->tmp[4], *r = op->tmp[5], *mmp = op->tmp[6], *y = op->tmp[7];
+  void *t = op->T(0), *z = op->T(1), *w = op->T(2), *u = op->T(3);
+  void *p = op->T(4), *r = op->T(5), *mmp = op->T(6), *y = op->T(7);
   auto mark = [&](int i) {
     if (ev) CK(cudaEventRecord(ev[i], s));
   };
@@ -749,7 +765,7 @@ int gbf_apply(gbf_op* op, int opcode, const void* const* src, void* const* dst, 
           CK(cudaMemcpyAsync(dst[i], src[i], 2 * op->half(), cudaMemcpyDeviceToDevice, s));
         } else if (opcode == GBF_IMPORT_PHYSICAL_FERMION_SOURCE) {
           // walls, then Dminus
-          void* t = op->tmp[2];  // tmp[2], tmp[3] form one contiguous full field
+          void* t = op->T(2);  // tmp[2], tmp[3] form one contiguous full field
           CK(cudaMemsetAsync(t, 0, 2 * op->half(), s));
           wall(op, src[i], t, 1, s);
           apply_one(op, GBF_DMINUS, t, dst[i], GBF_FULL, s);
@@ -768,6 +784,7 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
     if (!op || !src || !x || !prm) throw Fail(GBF_E_ARG, "null argument");
     if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
     ensure_ws(op);
+    for (int i = 0; i < 10; ++i) op->T(i);  // allocate before any graph capture
     cudaStream_t user = (cudaStream_t)stream;
     cudaStream_t s = op->stream;
     CK(cudaEventRecord(op->ev_in, user));
@@ -778,7 +795,7 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
     const void* srcD = (const char*)src + D * h;
     void* xC = (char*)x + C * h;
     void* xD = (char*)x + D * h;
-    void *p = op->tmp[4], *r = op->tmp[5], *y = op->tmp[7], *s1 = op->tmp[8], *tC = op->tmp[9], *u = op->tmp[3];
+    void *p = op->T(4), *r = op->T(5), *y = op->T(7), *s1 = op->T(8), *tC = op->T(9), *u = op->T(3);
     // ---- prepare: r = Mpc^+ (src_D - Dhop G_C src_C)  (R_ne, normal_equation.py:47-48) ----
     op->local(s, C, srcC, tC, op->G());
     op->dslash(s, D, false, tC, s1, op->none(), -1.0, srcD, 1.0);

@@ -26,16 +26,22 @@
 
 namespace gbf {
 
-template <int P, int LS, int LK>
+template <int P, int LS, int LK, bool LOOP>
 __global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_kernel(const DslashArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
-  extern __shared__ double smem_d[];
+  extern __shared__ __align__(16) double smem_d[];
   const Geo& g = a.g;
   if (a.check_done && a.ra.st->all_done) return;
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = n < g.N;
   const int p = a.out_parity, q = 1 - p;
+  double red_re = 0, red_im = 0;
+  // block-uniform loop over tiles of blockDim sites; LOOP = false when the
+  // grid covers every tile (one tile per block, no loop is compiled)
+  const long long ntiles = (g.N + blockDim.x - 1) / blockDim.x;
+  long long tile = blockIdx.x;
+  do {
+  const long long n = tile * blockDim.x + threadIdx.x;
+  const bool active = n < g.N;
   V res[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) res[k] = cz<R>();
@@ -129,25 +135,43 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_
     }
     store_spinor<P>(a.out, g.N, n, res);
   }
-  if (a.red) {
+  if (a.red && active) {
     double vr = 0, vi = 0;
-    if (active) {
-      if (a.red == 1) {
-        V yv[12];
-        load_spinor<P>(a.Y, g.N, n, yv);
-        site_dot<R>(yv, res, vr, vi);
-      } else {
-        vr = site_norm2<R>(res);
-      }
+    if (a.red == 1) {
+      V yv[12];
+      load_spinor<P>(a.Y, g.N, n, yv);
+      site_dot<R>(yv, res, vr, vi);
+    } else {
+      vr = site_norm2<R>(res);
     }
+    red_re += vr;
+    red_im += vi;
+  }
+  tile += gridDim.x;
+  } while (LOOP && tile < ntiles);
+  if (a.red) {
     double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
-    block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, sm);
+    block_reduce_finalize(a.ra, red_re, red_im, g.N5, g.Ls, g.nrhs, sm);
   }
 }
 
 // ---------------------------------------------------------------------------
 // host-side launcher
 // ---------------------------------------------------------------------------
+// Grid of a reducing launch: enough blocks to fill the GPU, few enough that
+// the last block's pass over the [block][rhs] partials stays short.
+long long reduce_grid(long long ntiles, int nrhs) {
+  static const int sms = [] {
+    int d = 0, c = 152;
+    if (cudaGetDevice(&d) == cudaSuccess) cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, d);
+    return c;
+  }();
+  long long cap = 4LL * sms;
+  const long long by_partials = 4096LL / (nrhs > 0 ? nrhs : 1);
+  if (by_partials > cap) cap = by_partials;
+  return ntiles < cap ? ntiles : cap;
+}
+
 int block_size_for(int N5, int LK) {
   // blockDim = S * N5 with S a power of two and blockDim <= 256
   int S = 1;
@@ -164,19 +188,29 @@ size_t dslash_smem_bytes(int P, int LK, int bd) {
   return s;
 }
 
-template <int P, int LS, int LK>
-static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
+template <int P, int LS, int LK, bool LOOP>
+static cudaError_t launch_tl(const DslashArgs& a, cudaStream_t st) {
   const int bd = block_size_for(a.g.N5, LK);
   if (bd <= 0) return cudaErrorInvalidValue;
-  const long long nb = (a.g.N + bd - 1) / bd;
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
   const size_t sm = dslash_smem_bytes(P, LK, bd);
-  auto k = dslash_kernel<P, LS, LK>;
+  auto k = dslash_kernel<P, LS, LK, LOOP>;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
   k<<<(unsigned)nb, bd, sm, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int P, int LS, int LK>
+static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
+  const int bd = block_size_for(a.g.N5, LK);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs) < ntiles;
+  return loop ? launch_tl<P, LS, LK, true>(a, st) : launch_tl<P, LS, LK, false>(a, st);
 }
 
 cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st) {

@@ -88,32 +88,50 @@ __device__ __forceinline__ void local_apply_thread(const LocalOp& l, int Vh, int
 
 // s-matrix op through shared memory.  Threads of one block hold complete
 // s-columns (blockDim is a multiple of N5, i5 = rhs*Ls + s fastest).
-// tile: 24*blockDim reals; mat: 2*Ls*Ls reals.  All threads must call.
+// tile: 24*blockDim reals, one contiguous spinor per thread so the s-column
+// is read back with 16-byte loads (the threads of one column read the same
+// address: shared-memory broadcast); mat: 2*Ls*Ls reals.  All threads call.
+template <typename R> struct Vec4;
+template <> struct Vec4<float> { using T = float4; };
+template <> struct Vec4<double> { using T = double2; };
+
 template <typename R>
 __device__ __forceinline__ void smat_apply_block(const R* mat_g, int Ls, R* tile, R* mat, cplx<R> (&v)[12], bool load_mat) {
+  using W = typename Vec4<R>::T;
+  constexpr int per = (int)(sizeof(W) / sizeof(R));  // reals per vector load
   const int t = threadIdx.x, bd = blockDim.x;
   if (load_mat)
     for (int k = t; k < 2 * Ls * Ls; k += bd) mat[k] = mat_g[k];
+  R* mine = tile + 24 * t;
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
-    tile[(2 * k) * bd + t] = v[k].x;
-    tile[(2 * k + 1) * bd + t] = v[k].y;
+    mine[2 * k] = v[k].x;
+    mine[2 * k + 1] = v[k].y;
   }
   __syncthreads();
   const int s = t % Ls;
-  const int base = t - s;
+  const R* col = tile + 24 * (t - s);
   const R* m0 = mat + s * Ls;
   const R* m1 = mat + Ls * Ls + s * Ls;
+  R acc[24];
 #pragma unroll
-  for (int k = 0; k < 12; ++k) {
-    const R* m = k < 6 ? m0 : m1;
-    R ax = 0, ay = 0;
-    for (int sp = 0; sp < Ls; ++sp) {
-      ax = fma(m[sp], tile[(2 * k) * bd + base + sp], ax);
-      ay = fma(m[sp], tile[(2 * k + 1) * bd + base + sp], ay);
+  for (int k = 0; k < 24; ++k) acc[k] = 0;
+  for (int sp = 0; sp < Ls; ++sp) {
+    const R a0 = m0[sp], a1 = m1[sp];
+    const W* src = reinterpret_cast<const W*>(col + 24 * sp);
+#pragma unroll
+    for (int q = 0; q < 24 / per; ++q) {
+      const W w = src[q];
+      const R* e = reinterpret_cast<const R*>(&w);
+#pragma unroll
+      for (int j = 0; j < per; ++j) {
+        const int k = q * per + j;
+        acc[k] = fma(k < 12 ? a0 : a1, e[j], acc[k]);
+      }
     }
-    v[k] = mk<R>(ax, ay);
   }
+#pragma unroll
+  for (int k = 0; k < 12; ++k) v[k] = mk<R>(acc[2 * k], acc[2 * k + 1]);
   __syncthreads();
 }
 
@@ -263,32 +281,35 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double v
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  int P2 = 1;
-  while (P2 < bd) P2 <<= 1;
-  for (int rhs = 0; rhs < nrhs; ++rhs) {
+  // The partials form a flat [block][rhs] array.  Thread t sums entries
+  // t, t + bd, t + 2bd, ... (coalesced); since bd is a multiple of nrhs all of
+  // them belong to rhs t % nrhs.  Then thread r < nrhs adds the bd/nrhs
+  // thread sums of its rhs in order.  Fixed order: bitwise reproducible.
+  {
+    const long long total = (long long)gridDim.x * nrhs;
     double ar = 0, ai = 0;
-    for (unsigned b = t; b < gridDim.x; b += bd) {
-      double2 q = __ldcg(r.partial + (size_t)b * nrhs + rhs);
+#pragma unroll 4
+    for (long long e = t; e < total; e += bd) {
+      const double2 q = __ldcg(r.partial + e);
       ar += q.x;
       ai += q.y;
     }
-    if (shfl) {
+    if (nrhs == 1 && shfl) {
       const double2 s = block_sum_shfl(ar, ai, sm);
-      if (t == 0) finalize(r, rhs, s.x, s.y);
+      if (t == 0) finalize(r, 0, s.x, s.y);
+    } else {
+      sm[t] = ar;
+      sm[bd + t] = ai;
       __syncthreads();
-      continue;
-    }
-    sm[t] = ar;
-    sm[bd + t] = ai;
-    __syncthreads();
-    for (int k = P2 >> 1; k >= 1; k >>= 1) {
-      if (t < k && t + k < bd) {
-        sm[t] += sm[t + k];
-        sm[bd + t] += sm[bd + t + k];
+      if (t < nrhs) {
+        double sr = 0, si = 0;
+        for (int j = t; j < bd; j += nrhs) {
+          sr += sm[j];
+          si += sm[bd + j];
+        }
+        finalize(r, t, sr, si);
       }
-      __syncthreads();
     }
-    if (t == 0) finalize(r, rhs, sm[0], sm[bd]);
     __syncthreads();
   }
   if (t == 0) {

@@ -23,6 +23,7 @@ struct DslashArgs {
 };
 cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st);
 int block_size_for(int N5, int LK);
+long long reduce_grid(long long ntiles, int nrhs);
 long long dslash_blocks(const Geo& g, int LK);
 
 // Site-local kernel on one parity (gbf_local.cu):

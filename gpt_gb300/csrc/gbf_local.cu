@@ -12,14 +12,18 @@ namespace gbf {
 // site-local op with optional CG pre-step (p = r + beta p):
 // bytes/site: A + (W read+write if pre) + out + (X) + clover (288 B FP32, 576 B FP64)
 // ---------------------------------------------------------------------------
-template <int P, int LK>
+template <int P, int LK, bool LOOP>
 __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
-  extern __shared__ double smem_d[];
+  extern __shared__ __align__(16) double smem_d[];
   const Geo& g = a.g;
   if (a.check_done && a.ra.st->all_done) return;
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double red_re = 0, red_im = 0;
+  const long long ntiles = (g.N + blockDim.x - 1) / blockDim.x;
+  long long tile = blockIdx.x;
+  do {
+  const long long n = tile * blockDim.x + threadIdx.x;
   const bool active = n < g.N;
   V v[12];
 #pragma unroll
@@ -62,19 +66,23 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
     }
     if (a.out) store_spinor<P>(a.out, g.N, n, v);
   }
-  if (a.red) {
+  if (a.red && active) {
     double vr = 0, vi = 0;
-    if (active) {
-      if (a.red == 1) {
-        V yv[12];
-        load_spinor<P>(a.Y, g.N, n, yv);
-        site_dot<R>(yv, v, vr, vi);
-      } else {
-        vr = site_norm2<R>(v);
-      }
+    if (a.red == 1) {
+      V yv[12];
+      load_spinor<P>(a.Y, g.N, n, yv);
+      site_dot<R>(yv, v, vr, vi);
+    } else {
+      vr = site_norm2<R>(v);
     }
+    red_re += vr;
+    red_im += vi;
+  }
+  tile += gridDim.x;
+  } while (LOOP && tile < ntiles);
+  if (a.red) {
     double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
-    block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, sm);
+    block_reduce_finalize(a.ra, red_re, red_im, g.N5, g.Ls, g.nrhs, sm);
   }
 }
 
@@ -85,19 +93,29 @@ static size_t local_smem(int P, int LK, int bd) {
   return s + 2 * (size_t)bd * 8;
 }
 
-template <int P, int LK>
-static cudaError_t launch_local_t(const LocalArgs& a, cudaStream_t st) {
+template <int P, int LK, bool LOOP>
+static cudaError_t launch_local_tl(const LocalArgs& a, cudaStream_t st) {
   const int bd = block_size_for(a.g.N5, LK);
   if (bd <= 0) return cudaErrorInvalidValue;
-  const long long nb = (a.g.N + bd - 1) / bd;
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
   const size_t sm = local_smem(P, LK, bd);
-  auto k = local_kernel<P, LK>;
+  auto k = local_kernel<P, LK, LOOP>;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
   k<<<(unsigned)nb, bd, sm, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int P, int LK>
+static cudaError_t launch_local_t(const LocalArgs& a, cudaStream_t st) {
+  const int bd = block_size_for(a.g.N5, LK);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs) < ntiles;
+  return loop ? launch_local_tl<P, LK, true>(a, st) : launch_local_tl<P, LK, false>(a, st);
 }
 
 cudaError_t launch_local(int P, const LocalArgs& a, cudaStream_t st) {
@@ -116,12 +134,12 @@ template <int P>
 __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
-  extern __shared__ double smem_d[];
+  extern __shared__ __align__(16) double smem_d[];
   const Geo& g = a.g;
   if (a.ra.st->all_done) return;
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double vr = 0;
-  if (n < g.N) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
     const int i5 = (int)(n % g.N5);
     const int rhs = i5 / g.Ls;
     const R al = (R)a.ra.st->alpha[rhs];
@@ -135,7 +153,7 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
       r[k] = mk<R>(fma(-al, m[k].x, r[k].x), fma(-al, m[k].y, r[k].y));
       x[k] = mk<R>(fma(al, p[k].x, x[k].x), fma(al, p[k].y, x[k].y));
     }
-    vr = site_norm2<R>(r);
+    vr += site_norm2<R>(r);
     store_spinor<P>(a.r, g.N, n, r);
     store_spinor<P>(a.x, g.N, n, x);
   }
@@ -145,7 +163,7 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
 cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st) {
   const int bd = block_size_for(a.g.N5, LOC_NONE);
   if (bd <= 0) return cudaErrorInvalidValue;
-  const long long nb = (a.g.N + bd - 1) / bd;
+  const long long nb = reduce_grid((a.g.N + bd - 1) / bd, a.g.nrhs);
   const size_t sm = 2 * (size_t)bd * 8;
   if (P == P64) cg_update_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P32) cg_update_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
@@ -161,11 +179,11 @@ template <int P>
 __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
-  extern __shared__ double smem_d[];
+  extern __shared__ __align__(16) double smem_d[];
   const Geo& g = a.g;
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double vr = 0, vi = 0;
-  if (n < g.N) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
     const int i5 = (int)(n % g.N5);
     const int rhs = i5 / g.Ls;
     V x[12], y[12], o[12];
@@ -175,7 +193,10 @@ __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
 #pragma unroll
       for (int k = 0; k < 12; ++k) y[k] = cz<R>();
     if (a.red == 3) {
-      site_dot<R>(x, y, vr, vi);
+      double dr, di;
+      site_dot<R>(x, y, dr, di);
+      vr += dr;
+      vi += di;
     } else {
       const V ac = mk<R>((R)a.a_re[rhs], (R)a.a_im[rhs]);
       const R bc = (R)a.b_re[rhs];
@@ -185,7 +206,7 @@ __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
         o[k] = mk<R>(fma(bc, y[k].x, t.x), fma(bc, y[k].y, t.y));
       }
       if (a.write) store_spinor<P>(a.out, g.N, n, o);
-      if (a.red == 2) vr = site_norm2<R>(o);
+      if (a.red == 2) vr += site_norm2<R>(o);
     }
   }
   if (a.red) block_reduce_finalize(a.ra, vr, vi, g.N5, g.Ls, g.nrhs, smem_d);
@@ -194,7 +215,8 @@ __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
 cudaError_t launch_blas(int P, const BlasArgs& a, cudaStream_t st) {
   const int bd = block_size_for(a.g.N5, LOC_NONE);
   if (bd <= 0) return cudaErrorInvalidValue;
-  const long long nb = (a.g.N + bd - 1) / bd;
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
   const size_t sm = 2 * (size_t)bd * 8;
   if (P == P64) blas_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P32) blas_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);

@@ -97,7 +97,8 @@ class fermion_operator(matrix_operator):
         h = ctypes.c_void_p()
         _lib.check(L.gbf_create(name.encode(), prec.code, ctypes.byref(s), ctypes.byref(h)))
         self.obj = h
-        _lib.check(L.gbf_update_gauge(self.obj, U.U.ctypes.data_as(ctypes.c_void_p), 0, core.stream_ptr()))
+        uptr, on_dev = U.ptr()
+        _lib.check(L.gbf_update_gauge(self.obj, ctypes.c_void_p(uptr), on_dev, core.stream_ptr()))
         self._register()
 
     def __del__(self):

@@ -10,17 +10,53 @@ from .. import core
 
 
 class gauge_field:
+    """Links U_mu(x) in the natural layout: a host numpy array
+    complex128 [4, V, 3, 3], or a device tensor (float64 view of the same
+    layout) for fields that never leave HBM."""
+
     def __init__(self, grid, U):
-        U = np.ascontiguousarray(U, dtype=np.complex128)
-        assert U.shape == (4, grid.gsites, 3, 3), U.shape
         self.grid = grid
-        self.U = U
+        self.device = None
+        if hasattr(U, "is_cuda") and U.is_cuda:
+            assert U.dtype.is_floating_point and U.numel() == 4 * grid.gsites * 18
+            self.device = U.contiguous()
+            self.U = None
+        else:
+            U = np.ascontiguousarray(U, dtype=np.complex128)
+            assert U.shape == (4, grid.gsites, 3, 3), U.shape
+            self.U = U
+
+    def ptr(self):
+        """(pointer, on_device) for gbf_update_gauge."""
+        if self.device is not None:
+            return self.device.data_ptr(), 1
+        return self.U.ctypes.data, 0
+
+    def host(self):
+        if self.U is None:
+            self.U = self.device.cpu().numpy().view(np.complex128).reshape(4, self.grid.gsites, 3, 3)
+        return self.U
 
     def __getitem__(self, mu):
-        return self.U[mu]
+        return self.host()[mu]
 
     def __len__(self):
         return 4
+
+
+def random_su3_device(grid, eps, seed):
+    """Same recipe as random_su3, generated in HBM by gbf_random_gauge
+    (counter-based Philox4x32-10 random numbers; a different stream than numpy)."""
+    import ctypes
+
+    import torch
+
+    from .. import _lib
+
+    U = torch.empty(4 * grid.gsites * 18, dtype=torch.float64, device="cuda")
+    dims = (ctypes.c_int * 4)(*grid.fdimensions)
+    _lib.check(_lib.load().gbf_random_gauge(dims, float(eps), int(seed), U.data_ptr(), core.stream_ptr()))
+    return gauge_field(grid, U)
 
 
 def unit(grid):
@@ -110,6 +146,7 @@ def plaquette(U):
     tot = 0.0
     for mu in range(4):
         for nu in range(mu):
-            P = U.U[mu] @ U.U[nu][fw[mu]] @ np.conj(np.swapaxes(U.U[mu][fw[nu]], 1, 2)) @ np.conj(np.swapaxes(U.U[nu], 1, 2))
+            H = U.host()
+            P = H[mu] @ H[nu][fw[mu]] @ np.conj(np.swapaxes(H[mu][fw[nu]], 1, 2)) @ np.conj(np.swapaxes(H[nu], 1, 2))
             tot += np.real(np.trace(P, axis1=1, axis2=2)).sum()
     return 2.0 * tot / V / 4 / 3 / 3

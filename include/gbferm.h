@@ -149,6 +149,15 @@ unsigned long long gbf_launch_count(void);
  * reals), 72 (FP32, 18 reals) or 48 (FP32, 12 reals, SU(3) links). */
 int gbf_link_bytes(const gbf_op* op);
 
+/* Synthetic inputs on the device, natural layout (benchmarks and serving;
+ * the reference's g.qcd.gauge.random / rng.cnormal use gpt's CPU RNG,
+ * lib/gpt/core/random.py:103-148): U = exp(i eps H) per link with H
+ * Hermitian traceless from complex-Gaussian entries, complex128 [4][V][3][3];
+ * and n_complex standard complex-Gaussian numbers.  Counter-based
+ * (Philox4x32-10), so the output depends only on (seed, index). */
+int gbf_random_gauge(const int* dims, double eps, unsigned long long seed, void* U, void* stream);
+int gbf_random_spinor(long long n_complex, unsigned long long seed, void* out, void* stream);
+
 /* |x|^2 of a field, allocating nothing (no counterpart in the reference).
  * For callers that cannot call cudaMalloc: a process whose free HBM belongs
  * to its own pool, or a latency-critical loop that must not take cudaMalloc's
