@@ -63,6 +63,22 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(ms, dist=None, device="cpu"):
+    """Max of a per-rank duration over all ranks (the whole job is as slow as
+    its slowest replica)."""
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if dist is not None and dist.is_available() and dist.is_initialized():
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, steps, max_ms):
+    """Units processed by all ranks per second: replicas, weak scaling."""
+    return world * steps / (max_ms / 1000.0)
+
+
 def run_profile_mobius(args):
     """Profiling case of the 5D multi-rhs path (about 4 GB on the device)."""
     import torch
@@ -521,12 +537,8 @@ def run_gbf(args, dims):
     n1 = L.gbf_launch_count()
     clk = clocks.stop()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[args.steps])
-    t_local = torch.tensor([total_ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
-    total_ms = float(t_local.item())
-    value = world * args.steps / (total_ms / 1000.0)
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[args.steps]), dist, "cuda")
+    value = whole_job_rate(world, args.steps, total_ms)
 
     # true residual of the last solve, FP64 on the device
     r = op.F_lattice()
@@ -559,11 +571,7 @@ def run_gbf(args, dims):
         h_dst.copy_(d_nat, non_blocking=True)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    t_e = torch.tensor([e2e_ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
-    e2e_value = world * e2e_steps / (float(t_e.item()) / 1000.0)
+    e2e_value = whole_job_rate(world, e2e_steps, max_over_ranks(e0.elapsed_time(e1), dist, "cuda"))
 
     # ---- plain FP64 eo2_ne CG ----
     xp = plain(src)  # warm-up (also builds the graph)

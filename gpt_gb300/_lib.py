@@ -82,6 +82,7 @@ def load():
     sig = {
         "gbf_create": (I, [ctypes.c_char_p, I, ctypes.POINTER(gbf_params), ctypes.POINTER(P)]),
         "gbf_update_gauge": (I, [P, P, I, P]),
+        "gbf_update_gauge_from": (I, [P, P, I, P, P]),
         "gbf_set_mass": (I, [P, D, D]),
         "gbf_delete": (I, [P]),
         "gbf_apply": (I, [P, I, PP, PP, I, I, P]),
@@ -97,6 +98,8 @@ def load():
         "gbf_stream_sync": (I, [P]),
         "gbf_launch_count": (ctypes.c_ulonglong, []),
         "gbf_link_bytes": (I, [P]),
+        "gbf_tune": (I, [P, P, ctypes.POINTER(ctypes.c_int), DP]),
+        "gbf_set_tuning": (I, [P, ctypes.POINTER(ctypes.c_int)]),
         "gbf_random_gauge": (I, [ctypes.POINTER(ctypes.c_int), D, ctypes.c_ulonglong, P, P]),
         "gbf_random_spinor": (I, [ctypes.c_longlong, ctypes.c_ulonglong, P, P]),
         "gbf_norm2_noalloc": (I, [I, P, ctypes.c_longlong, I, DP, P]),

@@ -100,6 +100,9 @@ struct gbf_op {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_chk[2] = {nullptr, nullptr};
   cudaGraphExec_t graph = nullptr;
   int graph_K = 0;
+  // block sizes chosen by gbf_tune (0: default): hop with a per-thread
+  // epilogue, hop with the s-matrix epilogue, site-local kernel, CG update
+  int tuned_bd[4] = {0, 0, 0, 0};
 
   size_t half() const { return (size_t)half_bytes(prec, g.N); }
   // workspace half field i; halves 2k and 2k+1 are one contiguous full field,
@@ -158,6 +161,7 @@ struct gbf_op {
     a.Y = Y;
     a.ra = red(fin);
     a.check_done = check_done;
+    a.bd = tuned_bd[(l1.kind == LOC_SMAT) ? 1 : 0];
     if (l2.kind == LOC_SMAT) throw Fail(GBF_E_ARG, "internal: smat on the X term");
     CK(launch_dslash(prec, LS, a, s));
     count_launch();
@@ -180,6 +184,7 @@ struct gbf_op {
     a.Y = Y;
     a.ra = red(fin);
     a.check_done = check_done;
+    a.bd = tuned_bd[2];
     CK(launch_local(prec, a, s));
     count_launch();
   }
@@ -191,6 +196,7 @@ struct gbf_op {
     a.x = x;
     a.p = p;
     a.ra = red(FIN_BETA);
+    a.bd = tuned_bd[3];
     CK(launch_cg_update(prec, a, s));
     count_launch();
   }
@@ -225,10 +231,17 @@ void setup_geo(gbf_op* op) {
     g.ph_re[m] = (float)p.boundary_phases[2 * m];
     g.ph_im[m] = (float)p.boundary_phases[2 * m + 1];
   }
+  g.fLh0 = FastDiv((unsigned)g.Lh0);
+  g.fL1 = FastDiv((unsigned)g.L[1]);
+  g.fL2 = FastDiv((unsigned)g.L[2]);
+  g.fN5 = FastDiv((unsigned)g.N5);
+  g.fLs = FastDiv((unsigned)g.Ls);
   op->g4 = g;
   op->g4.Ls = 1;
   op->g4.N5 = g.nrhs;
   op->g4.N = (long long)g.Vh * g.nrhs;
+  op->g4.fN5 = FastDiv((unsigned)g.nrhs);
+  op->g4.fLs = FastDiv(1u);
 }
 
 // Cayley s-matrices of the Mobius operator with constant b_s = b, c_s = c
@@ -384,6 +397,7 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
     if (N5 > 256) throw Fail(GBF_E_ARG, "Ls * n_rhs must be <= 256");
     long long V = (long long)p.dims[0] * p.dims[1] * p.dims[2] * p.dims[3];
     if (V / 2 * N5 > (1LL << 31) / 12) throw Fail(GBF_E_ARG, "field too large for 32-bit component indexing");
+    if (V / 2 * 80 >= (1LL << 31)) throw Fail(GBF_E_ARG, "lattice too large for 32-bit link and clover indexing");
     auto* op = new gbf_op;
     op->name = nm;
     op->mobius = mob;
@@ -429,8 +443,28 @@ int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus) {
   });
 }
 
+static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gbf_op* from, void* stream);
+
 int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream) {
-  return guarded([&] {
+  return guarded([&] { update_gauge_impl(op, U, on_device, nullptr, stream); });
+}
+
+int gbf_update_gauge_from(gbf_op* op, const void* U, int on_device, const gbf_op* clover_from, void* stream) {
+  return guarded([&] { update_gauge_impl(op, U, on_device, clover_from, stream); });
+}
+
+}  // extern "C"
+
+static bool clover_compatible(const gbf_op* a, const gbf_op* b) {
+  if (!a || !b || a->mobius || b->mobius || !a->has_clover || !b->has_clover || !b->gauge_set) return false;
+  for (int m = 0; m < 4; ++m)
+    if (a->par.dims[m] != b->par.dims[m]) return false;
+  return a->par.mass == b->par.mass && a->par.csw_r == b->par.csw_r && a->par.csw_t == b->par.csw_t &&
+         a->par.xi_0 == b->par.xi_0 && a->par.nu == b->par.nu && b->prec == P64;
+}
+
+static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gbf_op* from, void* stream) {
+  {
     if (!op || !U) throw Fail(GBF_E_ARG, "null argument");
     cudaStream_t s = (cudaStream_t)stream;
     const Geo& g = op->g;
@@ -465,7 +499,25 @@ int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream) {
     }
     if (LS != L32R) CK(launch_pack_links(LS, g, Ud, op->links, lam, ph, op->errbits, s));
     op->LS = LS;
-    if (op->has_clover) {
+    if (op->has_clover && clover_compatible(op, from)) {
+      // convert the source operator's clover and inverse instead of rebuilding
+      const size_t c64 = (size_t)2 * 36 * g.Vh * sizeof(double2);
+      const size_t c32 = (size_t)2 * 18 * g.Vh * sizeof(float4);
+      const size_t mine = op->prec == P64 ? c64 : c32;
+      if (!op->clov_mem) op->clov_mem = dmalloc(2 * mine);
+      if (op->prec == P64) {
+        CK(cudaMemcpyAsync(op->clov_mem, from->clov_mem, 2 * mine, cudaMemcpyDeviceToDevice, s));
+      } else {
+        // 4 blocks (clover, inverse) x (even, odd) of 18 float4 rows of Vh sites
+        CK(launch_clover_narrow(from->clov_mem, op->clov_mem, 4LL * 18, g.Vh, s));
+        count_launch();
+      }
+      const size_t perpar = mine / 2;
+      op->clov[0] = op->clov_mem;
+      op->clov[1] = (char*)op->clov_mem + perpar;
+      op->clov_inv[0] = (char*)op->clov_mem + mine;
+      op->clov_inv[1] = (char*)op->clov_mem + mine + perpar;
+    } else if (op->has_clover) {
       const size_t c64 = (size_t)2 * 36 * g.Vh * sizeof(double2);  // one of clover / inverse, both parities
       const size_t c32 = (size_t)2 * 18 * g.Vh * sizeof(float4);
       const size_t mine = op->prec == P64 ? c64 : c32;
@@ -494,8 +546,10 @@ int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream) {
     }
     op->gauge_set = true;
     if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
-  });
+  }
 }
+
+extern "C" {
 
 int gbf_field_bytes(const gbf_op* op, int which, size_t* bytes) {
   return guarded([&] {
@@ -887,6 +941,73 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
         res->kernel_launches[i] = kcount[i];
       }
     }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: time each block-size candidate of the four kernel classes on
+// scratch fields of this operator (CUDA events on the caller's stream) and
+// keep the fastest.  Candidates: blockDim = S * N5, S a power of two,
+// 32 <= blockDim <= 256 (or N5 itself when N5 > 128).
+// ---------------------------------------------------------------------------
+int gbf_tune(gbf_op* op, void* stream, int* out_bd, double* out_us) {
+  return guarded([&] {
+    if (!op || !out_bd) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    ensure_ws(op);
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int i = 0; i < 4; ++i) CK(cudaMemsetAsync(op->T(i), 0, op->half(), s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int N5 = op->g.N5;
+    std::vector<int> cand;
+    for (int S = 1; S * N5 <= 256; S *= 2)
+      if (S * N5 >= 32 || N5 > 128) cand.push_back(S * N5);
+    if (cand.empty()) cand.push_back(pick_bd(0, N5));
+    auto run = [&](int cls) {
+      switch (cls) {
+        case 0: op->dslash(s, 0, false, op->T(0), op->T(1), op->mobius ? op->none() : op->G()); break;
+        case 1: op->dslash(s, 0, false, op->T(0), op->T(1), op->G()); break;
+        case 2: op->local(s, 0, op->T(0), op->T(1), op->G()); break;
+        default: op->cg_update(s, op->T(0), op->T(1), op->T(2), op->T(3)); break;
+      }
+    };
+    for (int cls = 0; cls < 4; ++cls) {
+      out_bd[cls] = 0;
+      if (out_us) out_us[cls] = 0.0;
+      if (cls == 1 && !op->mobius) continue;
+      int best = cand[0];
+      float best_ms = 1e30f;
+      for (int bd : cand) {
+        op->tuned_bd[cls] = bd;
+        run(cls);  // warm-up
+        CK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; ++r) run(cls);
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = bd;
+        }
+      }
+      op->tuned_bd[cls] = best;
+      out_bd[cls] = best;
+      if (out_us) out_us[cls] = 1000.0 * best_ms / 3.0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+  });
+}
+
+int gbf_set_tuning(gbf_op* op, const int* bd) {
+  return guarded([&] {
+    if (!op || !bd) throw Fail(GBF_E_ARG, "null argument");
+    for (int i = 0; i < 4; ++i) op->tuned_bd[i] = bd[i] > 0 ? pick_bd(bd[i], op->g.N5) : 0;
+    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
   });
 }
 

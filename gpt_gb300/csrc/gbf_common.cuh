@@ -31,6 +31,21 @@ enum LocalKind { LOC_NONE = 0, LOC_CLOVER = 1, LOC_SMAT = 2, LOC_SCALAR = 3 };
 constexpr int kMaxLs = 32;
 constexpr int kMaxRhs = 16;
 
+// Division of a 32-bit unsigned n < 2^31 by a run-time constant d >= 1 as a
+// multiply-high and a shift (Granlund & Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994): with l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1,  n / d = (umulhi(n, m) + n) >> l.
+struct FastDiv {
+  unsigned d, m, l;
+  __host__ __device__ FastDiv() : d(1), m(1), l(0) {}
+  __host__ explicit FastDiv(unsigned dd) : d(dd) {
+    l = 0;
+    while ((1ull << l) < dd) ++l;
+    m = (unsigned)(((1ull << 32) * ((1ull << l) - dd)) / dd + 1);
+  }
+  __device__ __forceinline__ unsigned div(unsigned n) const { return (__umulhi(n, m) + n) >> l; }
+};
+
 // Geometry and run-time constants of one operator.
 struct Geo {
   int L[4];
@@ -39,10 +54,11 @@ struct Geo {
   int N5;       // inner extent = Ls * nrhs
   int Ls;       // 5th dimension (1 for Wilson-clover)
   int nrhs;
-  long long N;  // 5D sites per parity = Vh * N5
+  long long N;  // 5D sites per parity = Vh * N5 (12 N < 2^31 is checked at creation)
   // run-time link factors for reconstructed links: lambda_mu = -cc_mu/2 and phase_mu
   float lam[4];
   float ph_re[4], ph_im[4];
+  FastDiv fLh0, fL1, fL2, fN5, fLs;
 };
 
 template <typename R> struct C2;
@@ -81,39 +97,47 @@ __host__ __device__ inline long long half_bytes(int P, long long N) {
   return P == P64 ? 192 * N : (P == P32 ? 96 * N : 52 * N);
 }
 
+// Element indices are 32-bit: gbf_create checks 12 N < 2^31 (and the link and
+// clover extents), so `n + k N` never overflows and each address is a single
+// 32-bit multiply-add into a 64-bit pointer.
 template <int P> __device__ __forceinline__ void load_spinor(const void* base, long long N, long long n, cplx<typename SpinorT<P>::R> (&v)[12]);
 template <int P> __device__ __forceinline__ void store_spinor(void* base, long long N, long long n, const cplx<typename SpinorT<P>::R> (&v)[12]);
 
-template <> __device__ __forceinline__ void load_spinor<P64>(const void* base, long long N, long long n, double2 (&v)[12]) {
-  const double2* p = reinterpret_cast<const double2*>(base) + n;
+template <> __device__ __forceinline__ void load_spinor<P64>(const void* base, long long N_, long long n_, double2 (&v)[12]) {
+  const double2* p = reinterpret_cast<const double2*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
-  for (int k = 0; k < 12; ++k) v[k] = __ldg(p + k * N);
+  for (int k = 0; k < 12; ++k) v[k] = __ldg(p + (n + k * N));
 }
-template <> __device__ __forceinline__ void store_spinor<P64>(void* base, long long N, long long n, const double2 (&v)[12]) {
-  double2* p = reinterpret_cast<double2*>(base) + n;
+template <> __device__ __forceinline__ void store_spinor<P64>(void* base, long long N_, long long n_, const double2 (&v)[12]) {
+  double2* p = reinterpret_cast<double2*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
-  for (int k = 0; k < 12; ++k) p[k * N] = v[k];
+  for (int k = 0; k < 12; ++k) p[n + k * N] = v[k];
 }
-template <> __device__ __forceinline__ void load_spinor<P32>(const void* base, long long N, long long n, float2 (&v)[12]) {
-  const float4* p = reinterpret_cast<const float4*>(base) + n;
+template <> __device__ __forceinline__ void load_spinor<P32>(const void* base, long long N_, long long n_, float2 (&v)[12]) {
+  const float4* p = reinterpret_cast<const float4*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    float4 q = __ldg(p + k * N);
+    float4 q = __ldg(p + (n + k * N));
     v[2 * k] = make_float2(q.x, q.y);
     v[2 * k + 1] = make_float2(q.z, q.w);
   }
 }
-template <> __device__ __forceinline__ void store_spinor<P32>(void* base, long long N, long long n, const float2 (&v)[12]) {
-  float4* p = reinterpret_cast<float4*>(base) + n;
+template <> __device__ __forceinline__ void store_spinor<P32>(void* base, long long N_, long long n_, const float2 (&v)[12]) {
+  float4* p = reinterpret_cast<float4*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) p[k * N] = make_float4(v[2 * k].x, v[2 * k].y, v[2 * k + 1].x, v[2 * k + 1].y);
+  for (int k = 0; k < 6; ++k) p[n + k * N] = make_float4(v[2 * k].x, v[2 * k].y, v[2 * k + 1].x, v[2 * k + 1].y);
 }
-template <> __device__ __forceinline__ void load_spinor<P16>(const void* base, long long N, long long n, float2 (&v)[12]) {
-  const uint4* p = reinterpret_cast<const uint4*>(base) + n;
-  const float s = __ldg(reinterpret_cast<const float*>(reinterpret_cast<const uint4*>(base) + 3 * N) + n);
+template <> __device__ __forceinline__ void load_spinor<P16>(const void* base, long long N_, long long n_, float2 (&v)[12]) {
+  const uint4* p = reinterpret_cast<const uint4*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
+  const float s = __ldg(reinterpret_cast<const float*>(p + 3 * N) + n);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    uint4 q = __ldg(p + k * N);
+    uint4 q = __ldg(p + (n + k * N));
     const unsigned w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -123,12 +147,13 @@ template <> __device__ __forceinline__ void load_spinor<P16>(const void* base, l
     }
   }
 }
-template <> __device__ __forceinline__ void store_spinor<P16>(void* base, long long N, long long n, const float2 (&v)[12]) {
+template <> __device__ __forceinline__ void store_spinor<P16>(void* base, long long N_, long long n_, const float2 (&v)[12]) {
   float m = 0.f;
 #pragma unroll
   for (int k = 0; k < 12; ++k) m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
   const float inv = m > 0.f ? 1.f / m : 0.f;
-  uint4* p = reinterpret_cast<uint4*>(base) + n;
+  uint4* p = reinterpret_cast<uint4*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     unsigned w[4];
@@ -137,9 +162,9 @@ template <> __device__ __forceinline__ void store_spinor<P16>(void* base, long l
       __half2 h = __floats2half2_rn(v[4 * k + j].x * inv, v[4 * k + j].y * inv);
       w[j] = *reinterpret_cast<unsigned*>(&h);
     }
-    p[k * N] = make_uint4(w[0], w[1], w[2], w[3]);
+    p[n + k * N] = make_uint4(w[0], w[1], w[2], w[3]);
   }
-  reinterpret_cast<float*>(reinterpret_cast<uint4*>(base) + 3 * N)[n] = m;
+  reinterpret_cast<float*>(p + 3 * N)[n] = m;
 }
 
 // ---------------------------------------------------------------------------
@@ -159,18 +184,21 @@ template <int LS, typename R>
 __device__ __forceinline__ void load_link(const void* links, int Vh, int p, int mu, int cb, cplx<R> (&u)[9]);
 
 template <> __device__ __forceinline__ void load_link<L64, double>(const void* links, int Vh, int p, int mu, int cb, double2 (&u)[9]) {
-  const double2* b = reinterpret_cast<const double2*>(links) + (size_t)(p * 4 + mu) * 9 * Vh + cb;
+  const double2* b = reinterpret_cast<const double2*>(links);
+  const unsigned o = (unsigned)((p * 4 + mu) * 9) * (unsigned)Vh + (unsigned)cb;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (size_t)k * Vh);
+  for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (o + (unsigned)k * (unsigned)Vh));
 }
 template <> __device__ __forceinline__ void load_link<L32, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
-  const float2* b = reinterpret_cast<const float2*>(links) + (size_t)(p * 4 + mu) * 9 * Vh + cb;
+  const float2* b = reinterpret_cast<const float2*>(links);
+  const unsigned o = (unsigned)((p * 4 + mu) * 9) * (unsigned)Vh + (unsigned)cb;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (size_t)k * Vh);
+  for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (o + (unsigned)k * (unsigned)Vh));
 }
 template <> __device__ __forceinline__ void load_link<L32R, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
-  const float4* b = reinterpret_cast<const float4*>(links) + (size_t)(p * 4 + mu) * 3 * Vh + cb;
-  float4 a0 = __ldg(b), a1 = __ldg(b + Vh), a2 = __ldg(b + 2 * (size_t)Vh);
+  const float4* b = reinterpret_cast<const float4*>(links);
+  const unsigned o = (unsigned)((p * 4 + mu) * 3) * (unsigned)Vh + (unsigned)cb;
+  float4 a0 = __ldg(b + o), a1 = __ldg(b + (o + (unsigned)Vh)), a2 = __ldg(b + (o + 2u * (unsigned)Vh));
   u[0] = make_float2(a0.x, a0.y); u[1] = make_float2(a0.z, a0.w); u[2] = make_float2(a1.x, a1.y);
   u[3] = make_float2(a1.z, a1.w); u[4] = make_float2(a2.x, a2.y); u[5] = make_float2(a2.z, a2.w);
   // row2 = conj(row0 x row1)
@@ -214,12 +242,13 @@ template <typename R> __device__ __forceinline__ cplx<R> coefmadd(int code, R s,
 struct Coord { int x[4]; };
 __device__ __forceinline__ Coord cb_coords(const Geo& g, int cb, int p) {
   Coord c;
-  int xh = cb % g.Lh0;
-  int r = cb / g.Lh0;
-  c.x[1] = r % g.L[1];
-  r /= g.L[1];
-  c.x[2] = r % g.L[2];
-  c.x[3] = r / g.L[2];
+  const unsigned r0 = g.fLh0.div((unsigned)cb);
+  const int xh = cb - (int)r0 * g.Lh0;
+  const unsigned r1 = g.fL1.div(r0);
+  c.x[1] = (int)r0 - (int)r1 * g.L[1];
+  const unsigned r2 = g.fL2.div(r1);
+  c.x[2] = (int)r1 - (int)r2 * g.L[2];
+  c.x[3] = (int)r2;
   c.x[0] = 2 * xh + ((c.x[1] + c.x[2] + c.x[3] + p) & 1);
   return c;
 }

@@ -47,8 +47,8 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_
   for (int k = 0; k < 12; ++k) res[k] = cz<R>();
   int cb = 0;
   if (active) {
-    cb = (int)(n / g.N5);
-    const int i5 = (int)(n - (long long)cb * g.N5);
+    cb = (int)g.fN5.div((unsigned)n);
+    const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
     const Coord c = cb_coords(g, cb, p);
     const R sf = (R)a.sgn;
 #pragma unroll
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_
         }
         const int ycb = cb_index(g, y);
         V psi[12];
-        load_spinor<P>(a.in, g.N, (long long)ycb * g.N5 + i5, psi);
+        load_spinor<P>(a.in, g.N, (unsigned)ycb * (unsigned)g.N5 + i5, psi);
         // project: h_r = psi_r + s * coef_r * psi_perm(r), r = 0, 1
         const R s = fwd ? sf : -sf;
         V h[2][3];
@@ -180,6 +180,14 @@ int block_size_for(int N5, int LK) {
   return N5 > 256 ? -1 : S * N5;
 }
 
+int pick_bd(int requested, int N5) {
+  if (requested > 0 && requested <= 256 && requested % N5 == 0) {
+    const int S = requested / N5;
+    if ((S & (S - 1)) == 0) return requested;
+  }
+  return block_size_for(N5, 0);
+}
+
 size_t dslash_smem_bytes(int P, int LK, int bd) {
   size_t rb = (P == P64) ? 8 : 4;
   size_t s = 0;
@@ -190,7 +198,7 @@ size_t dslash_smem_bytes(int P, int LK, int bd) {
 
 template <int P, int LS, int LK, bool LOOP>
 static cudaError_t launch_tl(const DslashArgs& a, cudaStream_t st) {
-  const int bd = block_size_for(a.g.N5, LK);
+  const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
   const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
@@ -206,7 +214,7 @@ static cudaError_t launch_tl(const DslashArgs& a, cudaStream_t st) {
 
 template <int P, int LS, int LK>
 static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
-  const int bd = block_size_for(a.g.N5, LK);
+  const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
   const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs) < ntiles;

@@ -24,10 +24,10 @@ struct LocalOp {
 template <typename R> struct CloverLoad;
 template <> struct CloverLoad<double> {
   static __device__ __forceinline__ void block(const void* base, int Vh, int cb, int b, double (&c)[36]) {
-    const double2* p = reinterpret_cast<const double2*>(base) + cb + (size_t)18 * b * Vh;
+    const double2* p = reinterpret_cast<const double2*>(base) + ((unsigned)cb + 18u * (unsigned)b * (unsigned)Vh);
 #pragma unroll
     for (int k = 0; k < 18; ++k) {
-      double2 q = __ldg(p + (size_t)k * Vh);
+      double2 q = __ldg(p + (unsigned)k * (unsigned)Vh);
       c[2 * k] = q.x;
       c[2 * k + 1] = q.y;
     }
@@ -35,10 +35,10 @@ template <> struct CloverLoad<double> {
 };
 template <> struct CloverLoad<float> {
   static __device__ __forceinline__ void block(const void* base, int Vh, int cb, int b, float (&c)[36]) {
-    const float4* p = reinterpret_cast<const float4*>(base) + cb + (size_t)9 * b * Vh;
+    const float4* p = reinterpret_cast<const float4*>(base) + ((unsigned)cb + 9u * (unsigned)b * (unsigned)Vh);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      float4 q = __ldg(p + (size_t)k * Vh);
+      float4 q = __ldg(p + (unsigned)k * (unsigned)Vh);
       c[4 * k] = q.x; c[4 * k + 1] = q.y; c[4 * k + 2] = q.z; c[4 * k + 3] = q.w;
     }
   }

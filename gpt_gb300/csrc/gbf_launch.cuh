@@ -20,9 +20,12 @@ struct DslashArgs {
   const void* Y;
   RedArgs ra;
   int check_done;
+  int bd;  // block size (0: default); a multiple of N5 with a power-of-two quotient, <= 256
 };
 cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st);
 int block_size_for(int N5, int LK);
+// requested block size if valid for N5, else the default
+int pick_bd(int requested, int N5);
 long long reduce_grid(long long ntiles, int nrhs);
 long long dslash_blocks(const Geo& g, int LK);
 
@@ -43,6 +46,7 @@ struct LocalArgs {
   const void* Y;
   RedArgs ra;
   int check_done;
+  int bd;
 };
 cudaError_t launch_local(int P, const LocalArgs& a, cudaStream_t st);
 
@@ -54,6 +58,7 @@ struct CGUpdateArgs {
   void* x;
   const void* p;
   RedArgs ra;
+  int bd;
 };
 cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st);
 
@@ -87,5 +92,9 @@ cudaError_t launch_pack_links(int LS, const Geo& g, const double2* U, void* link
 // clover: natural gauge -> per parity clover and inverse (FP64 double2[36][Vh] and FP32 float4[18][Vh])
 cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double csw_r, double csw_t, void* c64, void* ci64,
                           void* c32, void* ci32, unsigned* err_bits, cudaStream_t st);
+
+// FP64 clover storage (double2 [2*nrows32][Vh]) -> FP32 (float4 [nrows32][Vh]);
+// nrows32 is a row count (18 per parity block), not an element count
+cudaError_t launch_clover_narrow(const void* src64, void* dst32, long long nrows32, int Vh, cudaStream_t st);
 
 }  // namespace gbf

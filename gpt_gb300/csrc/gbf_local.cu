@@ -30,10 +30,10 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
   for (int k = 0; k < 12; ++k) v[k] = cz<R>();
   int cb = 0;
   if (active) {
-    cb = (int)(n / g.N5);
+    cb = (int)g.fN5.div((unsigned)n);
     load_spinor<P>(a.A, g.N, n, v);
     if (a.pre) {
-      const int rhs = (int)(n - (long long)cb * g.N5) / g.Ls;
+      const int rhs = (int)g.fLs.div((unsigned)n - (unsigned)cb * (unsigned)g.N5);
       const R beta = (R)a.ra.st->beta[rhs];
       V w[12];
       load_spinor<P>(a.W, g.N, n, w);
@@ -95,7 +95,7 @@ static size_t local_smem(int P, int LK, int bd) {
 
 template <int P, int LK, bool LOOP>
 static cudaError_t launch_local_tl(const LocalArgs& a, cudaStream_t st) {
-  const int bd = block_size_for(a.g.N5, LK);
+  const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
   const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
@@ -111,7 +111,7 @@ static cudaError_t launch_local_tl(const LocalArgs& a, cudaStream_t st) {
 
 template <int P, int LK>
 static cudaError_t launch_local_t(const LocalArgs& a, cudaStream_t st) {
-  const int bd = block_size_for(a.g.N5, LK);
+  const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
   const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs) < ntiles;
@@ -140,8 +140,8 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
   double vr = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
-    const int i5 = (int)(n % g.N5);
-    const int rhs = i5 / g.Ls;
+    const unsigned i5 = (unsigned)n - g.fN5.div((unsigned)n) * (unsigned)g.N5;
+    const int rhs = (int)g.fLs.div(i5);
     const R al = (R)a.ra.st->alpha[rhs];
     V r[12], m[12], x[12], p[12];
     load_spinor<P>(a.r, g.N, n, r);
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
 }
 
 cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st) {
-  const int bd = block_size_for(a.g.N5, LOC_NONE);
+  const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long nb = reduce_grid((a.g.N + bd - 1) / bd, a.g.nrhs);
   const size_t sm = 2 * (size_t)bd * 8;
@@ -184,8 +184,8 @@ __global__ void __launch_bounds__(256) blas_kernel(const BlasArgs a) {
   double vr = 0, vi = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
-    const int i5 = (int)(n % g.N5);
-    const int rhs = i5 / g.Ls;
+    const unsigned i5 = (unsigned)n - g.fN5.div((unsigned)n) * (unsigned)g.N5;
+    const int rhs = (int)g.fLs.div(i5);
     V x[12], y[12], o[12];
     load_spinor<P>(a.x, g.N, n, x);
     if (a.y) load_spinor<P>(a.y, g.N, n, y);
@@ -602,6 +602,20 @@ cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double cs
   const long long V = 2LL * g.Vh;
   const unsigned nb = (unsigned)((V + 127) / 128);
   clover_kernel<<<nb, 128, 0, st>>>(g, U, sig, diag, csw_r, csw_t, (double2*)c64, (double2*)ci64, (float4*)c32, (float4*)ci32, err);
+  return cudaGetLastError();
+}
+
+__global__ void clover_narrow_kernel(const double2* src, float4* dst, long long nrows32, int Vh) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows32 * Vh) return;
+  const long long row = t / Vh, cb = t - row * Vh;
+  const double2 a = src[(2 * row) * Vh + cb], b = src[(2 * row + 1) * Vh + cb];
+  dst[row * Vh + cb] = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+}
+
+cudaError_t launch_clover_narrow(const void* src64, void* dst32, long long nrows32, int Vh, cudaStream_t st) {
+  const long long n = nrows32 * Vh;
+  clover_narrow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const double2*)src64, (float4*)dst32, nrows32, Vh);
   return cudaGetLastError();
 }
 

@@ -79,7 +79,7 @@ def _params_struct(name, p, dims, Ls, n_rhs):
 class fermion_operator(matrix_operator):
     """Native fermion operator (cgpt_fermion_operator analogue)."""
 
-    def __init__(self, name, U, params, precision=None, daggered=False):
+    def __init__(self, name, U, params, precision=None, daggered=False, clover_from=None):
         self.name = name
         self.U = U
         self.params = dict(params)
@@ -98,7 +98,10 @@ class fermion_operator(matrix_operator):
         _lib.check(L.gbf_create(name.encode(), prec.code, ctypes.byref(s), ctypes.byref(h)))
         self.obj = h
         uptr, on_dev = U.ptr()
-        _lib.check(L.gbf_update_gauge(self.obj, ctypes.c_void_p(uptr), on_dev, core.stream_ptr()))
+        if clover_from is not None:
+            _lib.check(L.gbf_update_gauge_from(self.obj, ctypes.c_void_p(uptr), on_dev, clover_from.obj, core.stream_ptr()))
+        else:
+            _lib.check(L.gbf_update_gauge(self.obj, ctypes.c_void_p(uptr), on_dev, core.stream_ptr()))
         self._register()
 
     def __del__(self):
@@ -158,7 +161,9 @@ class fermion_operator(matrix_operator):
 
     # ---- base.py:219-260 ----
     def converted(self, precision):
-        return type(self)(self.U, self.params, precision=precision, daggered=self.daggered)
+        # same links and clover at another precision: the clover term is
+        # converted from this operator instead of rebuilt
+        return type(self)(self.U, self.params, precision=precision, daggered=self.daggered, clover_from=self)
 
     def updated(self, U):
         return type(self)(U, self.params, precision=self.precision, daggered=self.daggered)
@@ -184,6 +189,13 @@ class fermion_operator(matrix_operator):
     def link_bytes(self):
         """Bytes per stored link (144 FP64, 72 FP32, 48 FP32 reconstruct-12)."""
         return _lib.load().gbf_link_bytes(self.obj)
+
+    def tune(self, force=False):
+        """Choose the kernels' block sizes for this operator by timing them
+        (or re-apply the cached choice); returns {"tag", "params", "results"}."""
+        from .. import tune as _tune
+
+        return _tune.tune(self, force=force)
 
     # native eo2_ne + CG on the device (gbf_solve_eo2ne_cg)
     def _solve_eo2ne_cg(self, dst, src, eps, maxiter, graph_iterations=0, profile=0):
@@ -235,8 +247,8 @@ def wilson_clover(U, params=None, **kw):
 
 
 class wilson_clover_operator(fermion_operator):
-    def __init__(self, U, params, precision=None, daggered=False):
-        super().__init__("wilson_clover", U, params, precision, daggered)
+    def __init__(self, U, params, precision=None, daggered=False, clover_from=None):
+        super().__init__("wilson_clover", U, params, precision, daggered, clover_from)
 
 
 def mobius(U, params=None, **kw):
@@ -252,7 +264,7 @@ def mobius(U, params=None, **kw):
 
 
 class mobius_operator(fermion_operator):
-    def __init__(self, U, params, precision=None, daggered=False):
+    def __init__(self, U, params, precision=None, daggered=False, clover_from=None):
         super().__init__("mobius", U, params, precision, daggered)
 
 

@@ -75,6 +75,13 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
  * memory.  Builds links, the clover term and its inverse on the device. */
 int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream);
 
+/* gbf_update_gauge for an operator that differs from `clover_from` only in
+ * precision (base.py:230-231 `converted`): the links are packed from U and
+ * the clover term and its inverse are converted from `clover_from` instead
+ * of being rebuilt.  Falls back to the full build when the two operators'
+ * geometry or clover parameters differ. */
+int gbf_update_gauge_from(gbf_op* op, const void* U, int on_device, const gbf_op* clover_from, void* stream);
+
 /* cgpt set_mass_fermion_operator (operators.cc:74-83). */
 int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus);
 
@@ -134,6 +141,17 @@ typedef struct {
   int kernel_launches[3];
 } gbf_cg_result;
 int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* p, gbf_cg_result* res, void* stream);
+
+/* Autotuner (the role of lib/gpt/core/auto_tune.py for this library): times
+ * the block-size candidates of the four kernel classes -- [0] hopping kernel
+ * with a per-thread epilogue, [1] hopping kernel with the Mobius s-matrix
+ * epilogue, [2] site-local kernel, [3] CG update -- on scratch fields of
+ * `op` and keeps the fastest for all later launches of `op`.  out_bd[4]
+ * receives the chosen block sizes (0 = class not used), out_us[4] (optional)
+ * the time per launch.  gbf_set_tuning applies block sizes found earlier
+ * (for example from a cache file) without timing. */
+int gbf_tune(gbf_op* op, void* stream, int* out_bd, double* out_us);
+int gbf_set_tuning(gbf_op* op, const int* bd);
 
 /* Thread-local message of the last error (exception.h:21-39 analogue). */
 const char* gbf_last_error(void);
