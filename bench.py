@@ -51,7 +51,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-dslash", action="store_true",
-                    help="profiling case: FP32 operator only, one inner eo2_ne CG of 12 iterations")
+                    help="profiling case: one operator only, one eo2_ne CG of 12 iterations")
+    ap.add_argument("--profile-precision", default="single", choices=["single", "double", "double_float"],
+                    help="precision of the --profile-dslash operator")
     ap.add_argument("--profile-mobius", action="store_true",
                     help="profiling case: FP32 mobius 12^3x24 Ls 12 with 12 packed rhs, 12 CG iterations")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
@@ -328,7 +330,8 @@ def run_profile_case(args, dims):
     grid = g.grid(dims, g.double)
     U = g.qcd.gauge.random_su3(grid, CFG["gauge_eps"], CFG["gauge_seed"])
     params = dict(mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"], boundary_phases=CFG["phases"])
-    op = g.qcd.fermion.wilson_clover_operator(U, params, precision=g.single)
+    prec = {"single": g.single, "double": g.double, "double_float": g.double_float}[args.profile_precision]
+    op = g.qcd.fermion.wilson_clover_operator(U, params, precision=prec)
     V = grid.gsites
     rng = np.random.default_rng(CFG["src_seed"])
     src = op.F_lattice()
@@ -339,7 +342,7 @@ def run_profile_case(args, dims):
     torch.cuda.synchronize()
     r = op._solve_eo2ne_cg(x, src, 1e-30, 12)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": "wilson_clover FP32 eo2_ne CG, 12 iterations", "lattice": dims,
+    print(json.dumps({"profile_case": f"wilson_clover {args.profile_precision} eo2_ne CG, 12 iterations", "lattice": dims,
                       "iterations": r.iterations, "link_bytes": op.link_bytes()}))
     return 0
 

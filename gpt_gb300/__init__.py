@@ -9,7 +9,7 @@ kernels of libgbferm.so (C ABI: include/gbferm.h).  PyTorch provides device
 memory and streams only.
 """
 from .core import (
-    precision, double, single, half, even, odd, full, grid, layout, lattice, vspincolor,
+    precision, double, single, half, double_float, even, odd, full, grid, layout, lattice, vspincolor,
     norm2, inner_product, axpy, axpby, copy, convert,
 )
 from . import _lib

@@ -9,7 +9,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libgbferm.so")
 
-GBF_DOUBLE, GBF_SINGLE, GBF_HALF = 0, 1, 2
+GBF_DOUBLE, GBF_SINGLE, GBF_HALF, GBF_DOUBLE_FLOAT = 0, 1, 2, 3
 GBF_EVEN, GBF_ODD, GBF_FULL = 0, 1, 2
 
 OPCODES = {

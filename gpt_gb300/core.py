@@ -29,6 +29,9 @@ class precision:
 double = precision("double", _lib.GBF_DOUBLE, 1e-15, 192)
 single = precision("single", _lib.GBF_SINGLE, 1e-7, 96)
 half = precision("half", _lib.GBF_HALF, 1e-3, 52)
+# FP64-class accuracy on the FP32 pipe: each real is h + l of two FP32 words
+# (no counterpart in the reference, whose precisions are single and double)
+double_float = precision("double_float", _lib.GBF_DOUBLE_FLOAT, 4e-15, 192)
 
 
 class checkerboard:

@@ -110,7 +110,7 @@ struct gbf_op {
   // the CG's vectors)
   void* T(int i);
   size_t half4() const { return (size_t)half_bytes(prec, g4.N); }
-  size_t rb() const { return prec == P64 ? 8 : 4; }
+  size_t rb() const { return (prec == P64 || prec == PDD) ? 8 : 4; }
 
   // ---- site-local operators ----
   LocalOp none() const { LocalOp l{}; l.kind = LOC_NONE; return l; }
@@ -311,6 +311,14 @@ void build_smat(gbf_op* op) {
   if (!op->smat) op->smat = dmalloc(all.size() * op->rb());
   if (op->prec == P64) {
     CK(cudaMemcpy(op->smat, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
+  } else if (op->prec == PDD) {
+    std::vector<float> f(2 * all.size());
+    for (size_t i = 0; i < all.size(); ++i) {
+      const dd v(all[i]);
+      f[2 * i] = v.h;
+      f[2 * i + 1] = v.l;
+    }
+    CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
   } else {
     std::vector<float> f(all.begin(), all.end());
     CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
@@ -373,7 +381,7 @@ unsigned long long gbf_launch_count(void) { return g_launches.load(); }
 
 int gbf_link_bytes(const gbf_op* op) {
   if (!op) return 0;
-  return op->LS == L64 ? 144 : (op->LS == L32 ? 72 : 48);
+  return (op->LS == L64 || op->LS == LDD) ? 144 : (op->LS == L32 ? 72 : 48);
 }
 
 int gbf_stream_sync(void* stream) {
@@ -386,7 +394,7 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
     *out = nullptr;
     std::string nm(name);
     if (nm != "wilson_clover" && nm != "mobius") throw Fail(GBF_E_UNSUPPORTED, "unknown fermion operator " + nm);
-    if (precision < GBF_DOUBLE || precision > GBF_HALF) throw Fail(GBF_E_ARG, "bad precision");
+    if (precision < GBF_DOUBLE || precision > GBF_DOUBLE_FLOAT) throw Fail(GBF_E_ARG, "bad precision");
     const gbf_params& p = *params;
     for (int m = 0; m < 4; ++m)
       if (p.dims[m] < 2 || p.dims[m] % 2) throw Fail(GBF_E_ARG, "lattice dimensions must be even and >= 2");
@@ -402,7 +410,7 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
     op->name = nm;
     op->mobius = mob;
     op->par = p;
-    op->prec = precision == GBF_DOUBLE ? P64 : (precision == GBF_SINGLE ? P32 : P16);
+    op->prec = precision == GBF_DOUBLE ? P64 : precision == GBF_SINGLE ? P32 : precision == GBF_HALF ? P16 : PDD;
     if (mob) {
       for (int m = 0; m < 4; ++m) op->cc[m] = 1.0;
       op->diag = 4.0 - p.M5;
@@ -460,7 +468,8 @@ static bool clover_compatible(const gbf_op* a, const gbf_op* b) {
   for (int m = 0; m < 4; ++m)
     if (a->par.dims[m] != b->par.dims[m]) return false;
   return a->par.mass == b->par.mass && a->par.csw_r == b->par.csw_r && a->par.csw_t == b->par.csw_t &&
-         a->par.xi_0 == b->par.xi_0 && a->par.nu == b->par.nu && b->prec == P64;
+         a->par.xi_0 == b->par.xi_0 && a->par.nu == b->par.nu && (b->prec == P64 || b->prec == PDD) &&
+         (b->prec == P64 || a->prec != P64);
 }
 
 static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gbf_op* from, void* stream) {
@@ -479,14 +488,15 @@ static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gb
     double lam[4], ph[8];
     for (int m = 0; m < 4; ++m) lam[m] = -0.5 * op->cc[m];
     for (int k = 0; k < 8; ++k) ph[k] = op->par.boundary_phases[k];
-    if (!op->links) op->links = dmalloc((size_t)8 * link_bytes_per_parity_mu(op->prec == P64 ? L64 : L32, g.Vh));
-    int LS = op->prec == P64 ? L64 : L32;
+    const bool wide = op->prec == P64 || op->prec == PDD;  // 8 bytes per real
+    if (!op->links) op->links = dmalloc((size_t)8 * link_bytes_per_parity_mu(wide ? L64 : L32, g.Vh));
+    int LS = op->prec == P64 ? L64 : (op->prec == PDD ? LDD : L32);
     // 12-real links save 24 B per link per output site, but cost a
     // reconstruction and a run-time phase in every thread.  When Ls * n_rhs
     // threads share each link (5D / multi-rhs fields) the link bytes are
     // already amortised and those flops would dominate: keep 18 reals.
     const bool try_r12 = op->par.reconstruct == 1 || (op->par.reconstruct != 0 && op->g.N5 < 4);
-    if (op->prec != P64 && try_r12) {
+    if (!wide && try_r12) {
       CK(cudaMemsetAsync(op->errbits, 0, sizeof(unsigned), s));
       CK(launch_pack_links(L32R, g, Ud, op->links, lam, ph, op->errbits, s));
       unsigned eb = 0;
@@ -503,13 +513,18 @@ static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gb
       // convert the source operator's clover and inverse instead of rebuilding
       const size_t c64 = (size_t)2 * 36 * g.Vh * sizeof(double2);
       const size_t c32 = (size_t)2 * 18 * g.Vh * sizeof(float4);
-      const size_t mine = op->prec == P64 ? c64 : c32;
+      const size_t mine = wide ? c64 : c32;
       if (!op->clov_mem) op->clov_mem = dmalloc(2 * mine);
-      if (op->prec == P64) {
+      if (op->prec == from->prec) {
         CK(cudaMemcpyAsync(op->clov_mem, from->clov_mem, 2 * mine, cudaMemcpyDeviceToDevice, s));
+      } else if (op->prec == PDD) {
+        // FP64 -> double-float, 4 x 36 complex per site pair
+        CK(launch_split_dd(from->clov_mem, op->clov_mem, 4LL * 36 * g.Vh, s));
+        count_launch();
       } else {
         // 4 blocks (clover, inverse) x (even, odd) of 18 float4 rows of Vh sites
-        CK(launch_clover_narrow(from->clov_mem, op->clov_mem, 4LL * 18, g.Vh, s));
+        if (from->prec == PDD) CK(launch_clover_narrow_dd(from->clov_mem, op->clov_mem, 4LL * 18, g.Vh, s));
+        else CK(launch_clover_narrow(from->clov_mem, op->clov_mem, 4LL * 18, g.Vh, s));
         count_launch();
       }
       const size_t perpar = mine / 2;
@@ -520,15 +535,22 @@ static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gb
     } else if (op->has_clover) {
       const size_t c64 = (size_t)2 * 36 * g.Vh * sizeof(double2);  // one of clover / inverse, both parities
       const size_t c32 = (size_t)2 * 18 * g.Vh * sizeof(float4);
-      const size_t mine = op->prec == P64 ? c64 : c32;
+      const size_t mine = wide ? c64 : c32;
       if (!op->clov_mem) op->clov_mem = dmalloc(2 * mine);
-      void* other = dmalloc(2 * (op->prec == P64 ? c32 : c64));
+      // the build writes FP64 and FP32 copies; a double-float operator builds
+      // both into scratch and splits the FP64 copy
+      void* other = dmalloc(2 * (op->prec == P64 ? c32 : op->prec == PDD ? c32 + c64 : c64));
       void *C64, *CI64, *C32, *CI32;
       if (op->prec == P64) { C64 = op->clov_mem; CI64 = (char*)op->clov_mem + c64; C32 = other; CI32 = (char*)other + c32; }
+      else if (op->prec == PDD) { C64 = other; CI64 = (char*)other + c64; C32 = (char*)other + 2 * c64; CI32 = (char*)other + 2 * c64 + c32; }
       else { C32 = op->clov_mem; CI32 = (char*)op->clov_mem + c32; C64 = other; CI64 = (char*)other + c64; }
       CK(cudaMemsetAsync(op->errbits + 1, 0, sizeof(unsigned), s));
       const double xi0 = op->par.xi_0 != 0.0 ? op->par.xi_0 : 1.0;
       CK(launch_clover(g, Ud, op->diag, op->par.csw_r / xi0, op->par.csw_t, C64, CI64, C32, CI32, op->errbits + 1, s));
+      if (op->prec == PDD) {
+        CK(launch_split_dd(C64, op->clov_mem, 4LL * 36 * g.Vh, s));  // C64 and CI64 are contiguous
+        count_launch();
+      }
       unsigned eb = 0;
       CK(cudaMemcpyAsync(&eb, op->errbits + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
@@ -759,6 +781,7 @@ static void wall(gbf_op* op, const void* in, void* out, int to5d, cudaStream_t s
     void* o = (char*)out + p * (to5d ? op->half() : op->half4());
     if (op->prec == P64) wall_kernel<P64><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
     else if (op->prec == P32) wall_kernel<P32><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
+    else if (op->prec == PDD) wall_kernel<PDD><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
     else wall_kernel<P16><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
     CK(cudaGetLastError());
     count_launch();

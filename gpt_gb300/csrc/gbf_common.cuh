@@ -24,8 +24,10 @@
 
 namespace gbf {
 
-enum Prec { P64 = 0, P32 = 1, P16 = 2 };
-enum LinkStore { L64 = 0, L32 = 1, L32R = 2 };
+// PDD: double-float storage and arithmetic (value = h + l, two FP32 words;
+// see struct dd below), the FP64-accurate path that runs on the FP32 pipe.
+enum Prec { P64 = 0, P32 = 1, P16 = 2, PDD = 3 };
+enum LinkStore { L64 = 0, L32 = 1, L32R = 2, LDD = 3 };
 enum LocalKind { LOC_NONE = 0, LOC_CLOVER = 1, LOC_SMAT = 2, LOC_SCALAR = 3 };
 
 constexpr int kMaxLs = 32;
@@ -84,6 +86,93 @@ template <typename R> __device__ __forceinline__ cplx<R> cmaddc(cplx<R> acc, cpl
   return acc;
 }
 template <typename R> __device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) { return cmadd<R>(cz<R>(), a, b); }
+template <typename R> __device__ __forceinline__ R rzero() { return R(0); }
+
+// ---------------------------------------------------------------------------
+// Double-float numbers.  A value is the unevaluated sum h + l of two FP32
+// words with |l| <= ulp(h)/2 after an addition or a product (a 48-bit
+// significand, unit roundoff 2^-48 ~ 3.6e-15), so FP64-class accuracy runs
+// on the FP32 pipe, which on GB300 issues about 70 times the FP64 pipe's
+// operations.  fma leaves the pair un-normalised (|l| a few ulp(h)): the
+// next operation absorbs it, and the saved fast-two-sum is a fifth of the
+// cost of an fma (build with GBF_DD_RENORM to normalise there too).
+// The operations are built from two error-free transformations:
+//   TwoSum(a, b) = (s, e), s = fl(a + b), s + e = a + b exactly
+//     (Knuth, TAOCP vol. 2, sec. 4.2.2, Theorem B);
+//   TwoProd(a, b) = (p, e), p = fl(a b), e = fma(a, b, -p), p + e = a b exactly.
+// Addition is the "sloppy" double-word sum and the product keeps the cross
+// terms a.h b.l + a.l b.h and drops a.l b.l (Joldes, Muller, Popescu, ACM
+// TOMS 44 (2017) 15, algorithms 4 and 10): the error of each operation is a
+// few 2^-48 relative to its operands.  Every intrinsic is round-to-nearest
+// and un-contracted, so the compiler cannot fuse or reorder the steps.
+// ---------------------------------------------------------------------------
+struct dd {
+  float h, l;
+  dd() = default;
+  __host__ __device__ constexpr dd(float hi, float lo) : h(hi), l(lo) {}
+  __host__ __device__ explicit dd(int a) : h((float)a), l(0.f) {}
+  __host__ __device__ explicit dd(float a) : h(a), l(0.f) {}
+  // round-to-nearest split of a double: h = fl32(a), l = fl32(a - h); a - h is exact
+  __host__ __device__ explicit dd(double a) : h((float)a), l((float)(a - (double)(float)a)) {}
+  __host__ __device__ explicit operator double() const { return (double)h + (double)l; }
+};
+
+__device__ __forceinline__ dd dd_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return dd(s, e);
+}
+// exact when |a| >= |b| (or a == 0)
+__device__ __forceinline__ dd dd_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return dd(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ dd operator-(dd a) { return dd(-a.h, -a.l); }
+__device__ __forceinline__ dd operator+(dd a, dd b) {
+  const dd s = dd_two_sum(a.h, b.h);
+  return dd_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
+__device__ __forceinline__ dd operator*(dd a, dd b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return dd_fast_two_sum(p, e);
+}
+// a * b + c
+using ::fma;
+__device__ __forceinline__ dd fma(dd a, dd b, dd c) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  const dd s = dd_two_sum(p, c.h);
+#ifdef GBF_DD_RENORM
+  return dd_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(e, c.l)));
+#else
+  return dd(s.h, __fadd_rn(s.l, __fadd_rn(e, c.l)));
+#endif
+}
+// exact scaling by +-1 (or any power of two)
+__device__ __forceinline__ dd dd_scale2(float f, dd a) { return dd(__fmul_rn(f, a.h), __fmul_rn(f, a.l)); }
+
+struct ddc {
+  dd x, y;
+};
+template <> struct C2<dd> { using T = ddc; };
+template <> __device__ __forceinline__ dd rzero<dd>() { return dd(0.f, 0.f); }
+template <> __device__ __forceinline__ cplx<dd> cz<dd>() { return mk<dd>(dd(0.f, 0.f), dd(0.f, 0.f)); }
+
+// Normalise an fma result before it is stored or used as a factor: with
+// cancellation in the un-normalised pair |l| can exceed |h|, and a product
+// (which drops l_a l_b) would then be wrong.  No-op for FP32 / FP64.
+template <typename R> __device__ __forceinline__ void nrm(cplx<R>&) {}
+template <> __device__ __forceinline__ void nrm<dd>(cplx<dd>& v) {
+  v.x = dd_fast_two_sum(v.x.h, v.x.l);
+  v.y = dd_fast_two_sum(v.y.h, v.y.l);
+}
 
 // ---------------------------------------------------------------------------
 // spinor storage
@@ -92,9 +181,10 @@ template <int P> struct SpinorT;
 template <> struct SpinorT<P64> { using R = double; static constexpr int bytes = 192; };
 template <> struct SpinorT<P32> { using R = float; static constexpr int bytes = 96; };
 template <> struct SpinorT<P16> { using R = float; static constexpr int bytes = 52; };
+template <> struct SpinorT<PDD> { using R = dd; static constexpr int bytes = 192; };
 
 __host__ __device__ inline long long half_bytes(int P, long long N) {
-  return P == P64 ? 192 * N : (P == P32 ? 96 * N : 52 * N);
+  return (P == P64 || P == PDD) ? 192 * N : (P == P32 ? 96 * N : 52 * N);
 }
 
 // Element indices are 32-bit: gbf_create checks 12 N < 2^31 (and the link and
@@ -114,6 +204,27 @@ template <> __device__ __forceinline__ void store_spinor<P64>(void* base, long l
   const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
   for (int k = 0; k < 12; ++k) p[n + k * N] = v[k];
+}
+// double-float: float4 (re.h, re.l, im.h, im.l) [12][N]
+template <> __device__ __forceinline__ void load_spinor<PDD>(const void* base, long long N_, long long n_, ddc (&v)[12]) {
+  const float4* p = reinterpret_cast<const float4*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    const float4 q = __ldg(p + (n + k * N));
+    v[k].x = dd(q.x, q.y);
+    v[k].y = dd(q.z, q.w);
+  }
+}
+template <> __device__ __forceinline__ void store_spinor<PDD>(void* base, long long N_, long long n_, const ddc (&v)[12]) {
+  float4* p = reinterpret_cast<float4*>(base);
+  const unsigned N = (unsigned)N_, n = (unsigned)n_;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    ddc w = v[k];
+    nrm<dd>(w);  // memory holds normalised pairs
+    p[n + k * N] = make_float4(w.x.h, w.x.l, w.y.h, w.y.l);
+  }
 }
 template <> __device__ __forceinline__ void load_spinor<P32>(const void* base, long long N_, long long n_, float2 (&v)[12]) {
   const float4* p = reinterpret_cast<const float4*>(base);
@@ -174,9 +285,10 @@ template <int LS> struct LinkT;
 template <> struct LinkT<L64> { using R = double; static constexpr int chunks = 9; static constexpr int chunk_bytes = 16; };
 template <> struct LinkT<L32> { using R = float; static constexpr int chunks = 9; static constexpr int chunk_bytes = 8; };
 template <> struct LinkT<L32R> { using R = float; static constexpr int chunks = 3; static constexpr int chunk_bytes = 16; };
+template <> struct LinkT<LDD> { using R = dd; static constexpr int chunks = 9; static constexpr int chunk_bytes = 16; };
 
 __host__ __device__ inline long long link_bytes_per_parity_mu(int LS, int Vh) {
-  return (long long)Vh * (LS == L64 ? 144 : (LS == L32 ? 72 : 48));
+  return (long long)Vh * ((LS == L64 || LS == LDD) ? 144 : (LS == L32 ? 72 : 48));
 }
 
 // Load U_mu at checkerboard index cb of parity p into u[9] (row major).
@@ -188,6 +300,16 @@ template <> __device__ __forceinline__ void load_link<L64, double>(const void* l
   const unsigned o = (unsigned)((p * 4 + mu) * 9) * (unsigned)Vh + (unsigned)cb;
 #pragma unroll
   for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (o + (unsigned)k * (unsigned)Vh));
+}
+template <> __device__ __forceinline__ void load_link<LDD, dd>(const void* links, int Vh, int p, int mu, int cb, ddc (&u)[9]) {
+  const float4* b = reinterpret_cast<const float4*>(links);
+  const unsigned o = (unsigned)((p * 4 + mu) * 9) * (unsigned)Vh + (unsigned)cb;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const float4 q = __ldg(b + (o + (unsigned)k * (unsigned)Vh));
+    u[k].x = dd(q.x, q.y);
+    u[k].y = dd(q.z, q.w);
+  }
 }
 template <> __device__ __forceinline__ void load_link<L32, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
   const float2* b = reinterpret_cast<const float2*>(links);
@@ -235,6 +357,39 @@ template <typename R> __device__ __forceinline__ cplx<R> coefmadd(int code, R s,
     case 1: return mk<R>(fma(-s, v.x, a.x), fma(-s, v.y, a.y));
     case 2: return mk<R>(fma(-s, v.y, a.x), fma(s, v.x, a.y));
     default: return mk<R>(fma(s, v.y, a.x), fma(-s, v.x, a.y));
+  }
+}
+// double-float: the callers' s is the projector sign +-1, so s*v is an exact
+// rescaling and the term is a double-float addition
+template <> __device__ __forceinline__ cplx<dd> coefmadd<dd>(int code, dd s, cplx<dd> v, cplx<dd> a) {
+  const dd vx = dd_scale2(s.h, v.x), vy = dd_scale2(s.h, v.y);
+  switch (code) {
+    case 0: return mk<dd>(a.x + vx, a.y + vy);
+    case 1: return mk<dd>(a.x - vx, a.y - vy);
+    case 2: return mk<dd>(a.x - vy, a.y + vx);
+    default: return mk<dd>(a.x + vy, a.y - vx);
+  }
+}
+
+// a + s * coef * v with the coefficient code and the sign known only at run
+// time (rolled direction loops): branch-free, s = +-1
+__device__ __forceinline__ cplx<dd> coefmadd_rt(int code, float s, cplx<dd> v, cplx<dd> a) {
+  const bool im = code >= 2;
+  const float sg = (code == 1 || code == 3) ? -s : s;
+  const dd tx = im ? -v.y : v.x;  // coef = +-i multiplies by i: (x, y) -> (-y, x)
+  const dd ty = im ? v.x : v.y;
+  return mk<dd>(a.x + dd_scale2(sg, tx), a.y + dd_scale2(sg, ty));
+}
+
+// the three colour components of spin k of a double-float spinor
+__device__ __forceinline__ void load_spin_dd(const void* base, long long N_, unsigned n, int k, ddc (&v)[3]) {
+  const float4* p = reinterpret_cast<const float4*>(base);
+  const unsigned N = (unsigned)N_;
+#pragma unroll
+  for (int col = 0; col < 3; ++col) {
+    const float4 q = __ldg(p + (n + (unsigned)(3 * k + col) * N));
+    v[col].x = dd(q.x, q.y);
+    v[col].y = dd(q.z, q.w);
   }
 }
 

@@ -23,11 +23,16 @@
 #ifndef GBF_DSLASH_MINB
 #define GBF_DSLASH_MINB 2
 #endif
+// the same for the double-float variant (2: 128 registers, a few spills in
+// the clover epilogue, measured faster than 1 block of 255 registers)
+#ifndef GBF_DSLASH_MINB_DD
+#define GBF_DSLASH_MINB_DD 2
+#endif
 
 namespace gbf {
 
 template <int P, int LS, int LK, bool LOOP>
-__global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_kernel(const DslashArgs a) {
+__global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MINB_DD : GBF_DSLASH_MINB)) dslash_kernel(const DslashArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
   extern __shared__ __align__(16) double smem_d[];
@@ -46,7 +51,68 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_
 #pragma unroll
   for (int k = 0; k < 12; ++k) res[k] = cz<R>();
   int cb = 0;
-  if (active) {
+  if constexpr (P == PDD) {
+   if (active) {
+    // double-float: the same hop with a rolled direction loop (one iteration
+    // is about 1.5k instructions; unrolled eight times the kernel would not
+    // fit the instruction cache)
+    cb = (int)g.fN5.div((unsigned)n);
+    const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
+    const Coord c = cb_coords(g, cb, p);
+#pragma unroll 1
+    for (int d = 0; d < 8; ++d) {
+      const int mu = d >> 1;
+      const bool fwd = (d & 1) == 0;
+      int y[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int xm = c.x[m], Lm = g.L[m];
+        y[m] = (m != mu) ? xm : fwd ? (xm == Lm - 1 ? 0 : xm + 1) : (xm == 0 ? Lm - 1 : xm - 1);
+      }
+      const int ycb = cb_index(g, y);
+      const unsigned site = (unsigned)ycb * (unsigned)g.N5 + i5;
+      const float s = fwd ? a.sgn : -a.sgn;
+      cplx<dd> h[2][3];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        cplx<dd> up[3], lo[3];
+        load_spin_dd(a.in, g.N, site, r, up);
+        load_spin_dd(a.in, g.N, site, gperm(mu, r), lo);
+        const int cr = gcoef(mu, r);
+#pragma unroll
+        for (int col = 0; col < 3; ++col) h[r][col] = coefmadd_rt(cr, s, lo[col], up[col]);
+      }
+      cplx<dd> u[9];
+      load_link<LDD, dd>(a.links, g.Vh, fwd ? p : q, mu, fwd ? cb : ycb, u);
+      cplx<dd> uh[2][3];
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          cplx<dd> acc = cz<dd>();
+#pragma unroll
+          for (int j = 0; j < 3; ++j) acc = fwd ? cmadd<dd>(acc, u[3 * i + j], h[r][j]) : cmaddc<dd>(acc, u[3 * j + i], h[r][j]);
+          uh[r][i] = acc;
+        }
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          res[3 * r + i] = add<dd>(res[3 * r + i], uh[r][i]);
+        }
+#pragma unroll
+      for (int r = 2; r < 4; ++r) {
+        const bool first = gperm(mu, r) == 0;
+        const int cr = gcoef(mu, r);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          cplx<dd>& t = res[3 * r + i];
+          t = coefmadd_rt(cr, s, first ? uh[0][i] : uh[1][i], t);
+        }
+      }
+    }
+   }
+  } else if (active) {
     cb = (int)g.fN5.div((unsigned)n);
     const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
     const Coord c = cb_coords(g, cb, p);
@@ -123,7 +189,10 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : GBF_DSLASH_MINB)) dslash_
     if (a.c1 != 1.0) {
       const R c1 = (R)a.c1;
 #pragma unroll
-      for (int k = 0; k < 12; ++k) res[k] = scl<R>(c1, res[k]);
+      for (int k = 0; k < 12; ++k) {
+        nrm<R>(res[k]);
+        res[k] = scl<R>(c1, res[k]);
+      }
     }
     if (a.X) {
       V xv[12];
@@ -189,7 +258,7 @@ int pick_bd(int requested, int N5) {
 }
 
 size_t dslash_smem_bytes(int P, int LK, int bd) {
-  size_t rb = (P == P64) ? 8 : 4;
+  size_t rb = (P == P64 || P == PDD) ? 8 : 4;
   size_t s = 0;
   if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
   s += 2 * (size_t)bd * 8;
@@ -233,6 +302,7 @@ cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st) {
   GBF_D(P32, L32R)
   GBF_D(P16, L32)
   GBF_D(P16, L32R)
+  GBF_D(PDD, LDD)
 #undef GBF_D
   return cudaErrorInvalidValue;
 }

@@ -2,6 +2,7 @@
 // site-local operators (clover, s-matrix), the deterministic block reduction
 // and its last-block finalisation, and the CG scalar updates.
 #pragma once
+#include <type_traits>
 #include "gbf_common.cuh"
 
 namespace gbf {
@@ -43,34 +44,55 @@ template <> struct CloverLoad<float> {
     }
   }
 };
+// double-float: the FP64 layout with each double2 stored as float4 (x.h, x.l, y.h, y.l)
+template <> struct CloverLoad<dd> {
+  static __device__ __forceinline__ void block(const void* base, int Vh, int cb, int b, dd (&c)[36]) {
+    const float4* p = reinterpret_cast<const float4*>(base) + ((unsigned)cb + 18u * (unsigned)b * (unsigned)Vh);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+      const float4 q = __ldg(p + (unsigned)k * (unsigned)Vh);
+      c[2 * k] = dd(q.x, q.y);
+      c[2 * k + 1] = dd(q.z, q.w);
+    }
+  }
+};
 
 // off-diagonal index of (i, j), i > j
 __host__ __device__ constexpr int tri(int i, int j) { return i * (i - 1) / 2 + j; }
 
+// The double-float variant keeps the two chiral blocks in a rolled loop (the
+// block is selected into w and written back by predicated moves): its fully
+// unrolled code would not fit the instruction cache.
 template <typename R>
 __device__ __forceinline__ void clover_apply(const void* base, int Vh, int cb, cplx<R> (&v)[12]) {
-#pragma unroll
+  constexpr bool kRoll = std::is_same<R, dd>::value;
+#pragma unroll(kRoll ? 1 : 2)
   for (int b = 0; b < 2; ++b) {
     R c[36];
     CloverLoad<R>::block(base, Vh, cb, b, c);
-    cplx<R> o[6];
+    cplx<R> w[6], o[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) w[i] = b ? v[6 + i] : v[i];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-      cplx<R> acc = scl<R>(c[i], v[6 * b + i]);
+      cplx<R> acc = scl<R>(c[i], w[i]);
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
         if (j < i) {
           const int t = tri(i, j);
-          acc = cmadd<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), v[6 * b + j]);
+          acc = cmadd<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), w[j]);
         } else if (j > i) {
           const int t = tri(j, i);
-          acc = cmaddc<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), v[6 * b + j]);
+          acc = cmaddc<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), w[j]);
         }
       }
       o[i] = acc;
     }
 #pragma unroll
-    for (int i = 0; i < 6; ++i) v[6 * b + i] = o[i];
+    for (int i = 0; i < 6; ++i) {
+      if (b) v[6 + i] = o[i];
+      else v[i] = o[i];
+    }
   }
 }
 
@@ -82,7 +104,10 @@ __device__ __forceinline__ void local_apply_thread(const LocalOp& l, int Vh, int
   } else if (l.kind == LOC_SCALAR) {
     const R s = (R)l.scalar;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) v[k] = scl<R>(s, v[k]);
+    for (int k = 0; k < 12; ++k) {
+      nrm<R>(v[k]);
+      v[k] = scl<R>(s, v[k]);
+    }
   }
 }
 
@@ -94,6 +119,7 @@ __device__ __forceinline__ void local_apply_thread(const LocalOp& l, int Vh, int
 template <typename R> struct Vec4;
 template <> struct Vec4<float> { using T = float4; };
 template <> struct Vec4<double> { using T = double2; };
+template <> struct Vec4<dd> { using T = float4; };
 
 template <typename R>
 __device__ __forceinline__ void smat_apply_block(const R* mat_g, int Ls, R* tile, R* mat, cplx<R> (&v)[12], bool load_mat) {
@@ -115,7 +141,7 @@ __device__ __forceinline__ void smat_apply_block(const R* mat_g, int Ls, R* tile
   const R* m1 = mat + Ls * Ls + s * Ls;
   R acc[24];
 #pragma unroll
-  for (int k = 0; k < 24; ++k) acc[k] = 0;
+  for (int k = 0; k < 24; ++k) acc[k] = rzero<R>();
   for (int sp = 0; sp < Ls; ++sp) {
     const R a0 = m0[sp], a1 = m1[sp];
     const W* src = reinterpret_cast<const W*>(col + 24 * sp);
@@ -154,6 +180,43 @@ __device__ __forceinline__ void site_dot(const cplx<R> (&a)[12], const cplx<R> (
 template <typename R>
 __device__ __forceinline__ double site_norm2(const cplx<R> (&a)[12]) {
   R r = 0;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    r = fma(a[k].x, a[k].x, r);
+    r = fma(a[k].y, a[k].y, r);
+  }
+  return (double)r;
+}
+template <>
+__device__ __forceinline__ void site_dot<dd>(const ddc (&a_)[12], const ddc (&b_)[12], double& re, double& im) {
+  ddc a[12], b[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    a[k] = a_[k];
+    b[k] = b_[k];
+    nrm<dd>(a[k]);
+    nrm<dd>(b[k]);
+  }
+  dd r = rzero<dd>(), i = rzero<dd>();
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    r = fma(a[k].x, b[k].x, r);
+    r = fma(a[k].y, b[k].y, r);
+    i = fma(a[k].x, b[k].y, i);
+    i = fma(-a[k].y, b[k].x, i);
+  }
+  re = (double)r;
+  im = (double)i;
+}
+template <>
+__device__ __forceinline__ double site_norm2<dd>(const ddc (&a_)[12]) {
+  ddc a[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    a[k] = a_[k];
+    nrm<dd>(a[k]);
+  }
+  dd r = rzero<dd>();
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
     r = fma(a[k].x, a[k].x, r);

@@ -38,7 +38,10 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
       V w[12];
       load_spinor<P>(a.W, g.N, n, w);
 #pragma unroll
-      for (int k = 0; k < 12; ++k) v[k] = mk<R>(fma(beta, w[k].x, v[k].x), fma(beta, w[k].y, v[k].y));
+      for (int k = 0; k < 12; ++k) {
+        v[k] = mk<R>(fma(beta, w[k].x, v[k].x), fma(beta, w[k].y, v[k].y));
+        nrm<R>(v[k]);  // a factor of the local op below
+      }
       store_spinor<P>(a.W, g.N, n, v);
     }
   }
@@ -55,7 +58,10 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
     if (a.c1 != 1.0) {
       const R c1 = (R)a.c1;
 #pragma unroll
-      for (int k = 0; k < 12; ++k) v[k] = scl<R>(c1, v[k]);
+      for (int k = 0; k < 12; ++k) {
+        nrm<R>(v[k]);
+        v[k] = scl<R>(c1, v[k]);
+      }
     }
     if (a.X) {
       V xv[12];
@@ -87,7 +93,7 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
 }
 
 static size_t local_smem(int P, int LK, int bd) {
-  size_t rb = (P == P64) ? 8 : 4;
+  size_t rb = (P == P64 || P == PDD) ? 8 : 4;
   size_t s = 0;
   if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
   return s + 2 * (size_t)bd * 8;
@@ -123,6 +129,7 @@ cudaError_t launch_local(int P, const LocalArgs& a, cudaStream_t st) {
   if (P == P64) return sm ? launch_local_t<P64, LOC_SMAT>(a, st) : launch_local_t<P64, LOC_CLOVER>(a, st);
   if (P == P32) return sm ? launch_local_t<P32, LOC_SMAT>(a, st) : launch_local_t<P32, LOC_CLOVER>(a, st);
   if (P == P16) return sm ? launch_local_t<P16, LOC_SMAT>(a, st) : launch_local_t<P16, LOC_CLOVER>(a, st);
+  if (P == PDD) return sm ? launch_local_t<PDD, LOC_SMAT>(a, st) : launch_local_t<PDD, LOC_CLOVER>(a, st);
   return cudaErrorInvalidValue;
 }
 
@@ -168,6 +175,7 @@ cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st) {
   if (P == P64) cg_update_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P32) cg_update_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P16) cg_update_kernel<P16><<<(unsigned)nb, bd, sm, st>>>(a);
+  else if (P == PDD) cg_update_kernel<PDD><<<(unsigned)nb, bd, sm, st>>>(a);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
@@ -221,6 +229,7 @@ cudaError_t launch_blas(int P, const BlasArgs& a, cudaStream_t st) {
   if (P == P64) blas_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P32) blas_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P16) blas_kernel<P16><<<(unsigned)nb, bd, sm, st>>>(a);
+  else if (P == PDD) blas_kernel<PDD><<<(unsigned)nb, bd, sm, st>>>(a);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
@@ -250,6 +259,8 @@ cudaError_t launch_convert(int Pout, void* out, int Pin, const void* in, long lo
   GBF_CV(P64, P64) GBF_CV(P64, P32) GBF_CV(P64, P16)
   GBF_CV(P32, P64) GBF_CV(P32, P32) GBF_CV(P32, P16)
   GBF_CV(P16, P64) GBF_CV(P16, P32) GBF_CV(P16, P16)
+  GBF_CV(PDD, P64) GBF_CV(PDD, P32) GBF_CV(PDD, P16) GBF_CV(PDD, PDD)
+  GBF_CV(P64, PDD) GBF_CV(P32, PDD) GBF_CV(P16, PDD)
 #undef GBF_CV
   return cudaErrorInvalidValue;
 }
@@ -317,6 +328,7 @@ cudaError_t launch_import(int P, const Geo& g, const double2* nat, void* full, i
   if (P == P64) import_kernel<P64><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
   else if (P == P32) import_kernel<P32><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
   else if (P == P16) import_kernel<P16><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
+  else if (P == PDD) import_kernel<PDD><<<nb, 256, 0, st>>>(g, nat, full, rhs, to_natural);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
@@ -389,6 +401,12 @@ __global__ void pack_links_kernel(Geo g, const double2* U, void* links, LamPh la
   if (LS == L64) {
     double2* b = reinterpret_cast<double2*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
     for (int k = 0; k < 9; ++k) b[(size_t)k * g.Vh] = u[k];
+  } else if (LS == LDD) {
+    float4* b = reinterpret_cast<float4*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
+    for (int k = 0; k < 9; ++k) {
+      const dd re(u[k].x), im(u[k].y);
+      b[(size_t)k * g.Vh] = make_float4(re.h, re.l, im.h, im.l);
+    }
   } else {
     float2* b = reinterpret_cast<float2*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
     for (int k = 0; k < 9; ++k) b[(size_t)k * g.Vh] = make_float2((float)u[k].x, (float)u[k].y);
@@ -404,6 +422,7 @@ cudaError_t launch_pack_links(int LS, const Geo& g, const double2* U, void* link
   if (LS == L64) pack_links_kernel<L64><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
   else if (LS == L32) pack_links_kernel<L32><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
   else if (LS == L32R) pack_links_kernel<L32R><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
+  else if (LS == LDD) pack_links_kernel<LDD><<<nb, 256, 0, st>>>(g, U, links, lp[0], lp[1], lp[2], lp[3], err);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
@@ -616,6 +635,34 @@ __global__ void clover_narrow_kernel(const double2* src, float4* dst, long long 
 cudaError_t launch_clover_narrow(const void* src64, void* dst32, long long nrows32, int Vh, cudaStream_t st) {
   const long long n = nrows32 * Vh;
   clover_narrow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const double2*)src64, (float4*)dst32, nrows32, Vh);
+  return cudaGetLastError();
+}
+
+// double-float source: each double2 of the FP64 layout is a float4 (x.h, x.l, y.h, y.l)
+__global__ void clover_narrow_dd_kernel(const float4* src, float4* dst, long long nrows32, int Vh) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows32 * Vh) return;
+  const long long row = t / Vh, cb = t - row * Vh;
+  const float4 a = src[(2 * row) * Vh + cb], b = src[(2 * row + 1) * Vh + cb];
+  dst[row * Vh + cb] = make_float4(__fadd_rn(a.x, a.y), __fadd_rn(a.z, a.w), __fadd_rn(b.x, b.y), __fadd_rn(b.z, b.w));
+}
+
+cudaError_t launch_clover_narrow_dd(const void* srcdd, void* dst32, long long nrows32, int Vh, cudaStream_t st) {
+  const long long n = nrows32 * Vh;
+  clover_narrow_dd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const float4*)srcdd, (float4*)dst32, nrows32, Vh);
+  return cudaGetLastError();
+}
+
+__global__ void split_dd_kernel(const double2* src, float4* dst, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double2 a = src[t];
+  const dd x(a.x), y(a.y);
+  dst[t] = make_float4(x.h, x.l, y.h, y.l);
+}
+
+cudaError_t launch_split_dd(const void* src64, void* dst, long long n_complex, cudaStream_t st) {
+  split_dd_kernel<<<(unsigned)((n_complex + 255) / 256), 256, 0, st>>>((const double2*)src64, (float4*)dst, n_complex);
   return cudaGetLastError();
 }
 

@@ -70,7 +70,7 @@ thread_local std::string g_noalloc_err;
 }  // namespace
 
 extern "C" int gbf_norm2_noalloc(int precision, const void* x, long long n_sites, int nhalves, double* out, void* stream) {
-  if (!x || !out || n_sites < 0 || (nhalves != 1 && nhalves != 2) || precision < GBF_DOUBLE || precision > GBF_HALF) {
+  if (!x || !out || n_sites < 0 || (nhalves != 1 && nhalves != 2) || precision < GBF_DOUBLE || precision > GBF_DOUBLE_FLOAT) {
     g_noalloc_err = "gbf_norm2_noalloc: bad argument";
     return GBF_E_ARG;
   }
@@ -101,7 +101,9 @@ extern "C" int gbf_norm2_noalloc(int precision, const void* x, long long n_sites
   }
   NoAllocScratch* s = reinterpret_cast<NoAllocScratch*>(addr);
   cudaStream_t st = (cudaStream_t)stream;
-  const int P = precision == GBF_DOUBLE ? gbf::P64 : (precision == GBF_SINGLE ? gbf::P32 : gbf::P16);
+  const int P = precision == GBF_DOUBLE ? gbf::P64
+              : precision == GBF_SINGLE ? gbf::P32
+              : precision == GBF_HALF ? gbf::P16 : gbf::PDD;
   const long long half = gbf::half_bytes(P, n_sites);
   double total = 0.0;
   for (int h = 0; h < nhalves; ++h) {
@@ -113,6 +115,7 @@ extern "C" int gbf_norm2_noalloc(int precision, const void* x, long long n_sites
         const void* xh = (const char*)x + h * half;
         if (P == gbf::P64) norm2_noalloc_kernel<gbf::P64><<<nb, kNoAllocBlock, 0, st>>>(xh, n_sites, s);
         else if (P == gbf::P32) norm2_noalloc_kernel<gbf::P32><<<nb, kNoAllocBlock, 0, st>>>(xh, n_sites, s);
+        else if (P == gbf::PDD) norm2_noalloc_kernel<gbf::PDD><<<nb, kNoAllocBlock, 0, st>>>(xh, n_sites, s);
         else norm2_noalloc_kernel<gbf::P16><<<nb, kNoAllocBlock, 0, st>>>(xh, n_sites, s);
         e = cudaGetLastError();
       }

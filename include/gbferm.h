@@ -35,8 +35,13 @@ extern "C" {
 
 typedef struct gbf_op gbf_op;
 
-/* precision (cgpt: "single" / "double", operators.cc:36-57) */
-enum { GBF_DOUBLE = 0, GBF_SINGLE = 1, GBF_HALF = 2 };
+/* precision (cgpt: "single" / "double", operators.cc:36-57).  GBF_HALF: FP16
+ * spinors with a per-site FP32 scale, FP32 arithmetic.  GBF_DOUBLE_FLOAT (no
+ * counterpart in the reference): spinors, links, clover and arithmetic in
+ * double-float numbers, value = h + l of two FP32 words (48-bit significand,
+ * relative rounding ~2^-48 per operation), the same 8 bytes per real as FP64;
+ * FP64-class results computed on the FP32 pipe. */
+enum { GBF_DOUBLE = 0, GBF_SINGLE = 1, GBF_HALF = 2, GBF_DOUBLE_FLOAT = 3 };
 /* checkerboards (lib/gpt/core/checkerboard.py:22-25) */
 enum { GBF_EVEN = 0, GBF_ODD = 1, GBF_FULL = 2 };
 /* error classes */

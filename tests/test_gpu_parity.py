@@ -23,7 +23,10 @@ if not torch.cuda.is_available():  # collected on CPU hosts, skipped there
 import gpt_gb300 as g  # noqa: E402
 
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
-TOL = {"double": 1e-13, "single": 1e-6}
+# double_float (h + l of two FP32 words, 48-bit significand) is held to the
+# FP64 tolerance
+TOL = {"double": 1e-13, "double_float": 1e-13, "single": 1e-6}
+PREC = {"double": g.double, "double_float": g.double_float, "single": g.single}
 
 
 def rel(a, b):
@@ -67,13 +70,14 @@ def _fp_fields(dims, Ls=None):
     return f
 
 
+@pytest.mark.parametrize("prec", ["double", "double_float"])
 @pytest.mark.parametrize("name", ["wilson", "wilson_clover"])
-def test_gpu_wilson_clover_fingerprints(name):
+def test_gpu_wilson_clover_fingerprints(name, prec):
     fp = GOLD["fingerprints"]
     dims = fp["grid"]
     case = fp[name]
     f = _fp_fields(dims)
-    op = gpu_op("wilson_clover", f["U"], dims, g.double, **case["params"])
+    op = gpu_op("wilson_clover", f["U"], dims, PREC[prec], **case["params"])
     src = to_gpu(op, f["src4"])
     for tag, ref in case["matrices"].items():
         dst = op.M(src) if tag == "" else op.Mdiag(src)
@@ -81,13 +85,14 @@ def test_gpu_wilson_clover_fingerprints(name):
         assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (name, tag, X)
 
 
+@pytest.mark.parametrize("prec", ["double", "double_float"])
 @pytest.mark.parametrize("name", ["mobius", "mobius_axial_mass"])
-def test_gpu_mobius_fingerprints(name):
+def test_gpu_mobius_fingerprints(name, prec):
     fp = GOLD["fingerprints"]
     dims = fp["grid"]
     case = fp[name]
     f = _fp_fields(dims, case["params"]["Ls"])
-    op = gpu_op("mobius", f["U"], dims, g.double, **case["params"])
+    op = gpu_op("mobius", f["U"], dims, PREC[prec], **case["params"])
     src5 = to_gpu(op, f["src5"])
     src4 = to_gpu(op, f["src4"], five=False)
     for tag, ref in case["matrices"].items():
@@ -115,7 +120,7 @@ def _oracle(kind, U, dims, p):
     return o.mobius(U, dims, **{k: v for k, v in p.items() if k != "n_rhs"})
 
 
-@pytest.mark.parametrize("prec", ["double", "single"])
+@pytest.mark.parametrize("prec", ["double", "double_float", "single"])
 @pytest.mark.parametrize("kind,params,dims", [
     ("wilson_clover", WC, [4, 4, 4, 8]),
     ("wilson_clover", WC_ANISO, [4, 2, 6, 4]),
@@ -123,7 +128,7 @@ def _oracle(kind, U, dims, p):
     ("mobius", MOB, [4, 4, 2, 4]),
 ])
 def test_opcodes_vs_oracle(kind, params, dims, prec):
-    P = g.double if prec == "double" else g.single
+    P = PREC[prec]
     tol = TOL[prec]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 11).U
     ref = _oracle(kind, U, dims, params)
@@ -147,9 +152,9 @@ def test_opcodes_vs_oracle(kind, params, dims, prec):
             assert rel(dst[:], want) < tol, (name, sp)
 
 
-@pytest.mark.parametrize("prec", ["double", "single"])
+@pytest.mark.parametrize("prec", ["double", "double_float", "single"])
 def test_mobius_import_export(prec):
-    P = g.double if prec == "double" else g.single
+    P = PREC[prec]
     dims = [4, 4, 4, 4]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 3).U
     ref = _oracle("mobius", U, dims, MOB)
@@ -191,12 +196,13 @@ def test_multi_rhs_packed_equals_single():
 # ---------------------------------------------------------------------------
 # solvers
 # ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["double", "double_float"])
 @pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1))])
-def test_eo2ne_cg_vs_oracle(kind, params):
+def test_eo2ne_cg_vs_oracle(kind, params, prec):
     dims = [4, 4, 4, 8]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 21).U
     ref = _oracle(kind, U, dims, params)
-    op = gpu_op(kind, U, dims, g.double, **params)
+    op = gpu_op(kind, U, dims, PREC[prec], **params)
     b = rand_field(ref.shape(), 9)
     x_ref, it_ref, _ = ref.eo2ne_cg(b, 1e-10, 2000)
     inv = g.algorithms.inverter
@@ -211,16 +217,17 @@ def test_eo2ne_cg_vs_oracle(kind, params):
     assert rel(x, x_ref) < 1e-8
 
 
-def test_mixed_precision_defect_correction():
+@pytest.mark.parametrize("outer", ["double", "double_float"])
+def test_mixed_precision_defect_correction(outer):
     dims = [4, 4, 4, 8]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.3, 2).U
     ref = o.wilson_clover(U, dims, **dict(WC, mass=0.05))
-    op = gpu_op("wilson_clover", U, dims, g.double, **dict(WC, mass=0.05))
+    op = gpu_op("wilson_clover", U, dims, PREC[outer], **dict(WC, mass=0.05))
     b = rand_field(ref.shape(), 4)
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
     inner = inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": 1e-5, "maxiter": 1000}))
-    dc = inv.defect_correcting(inv.mixed_precision(inner, g.single, g.double), eps=1e-10, maxiter=20)
+    dc = inv.defect_correcting(inv.mixed_precision(inner, g.single, PREC[outer]), eps=1e-10, maxiter=20)
     slv = dc(op)
     x = slv(to_gpu(op, b))[:]
     r = b - ref.apply("M", x)
