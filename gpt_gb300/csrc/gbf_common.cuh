@@ -9,6 +9,7 @@
 //     FP32: float4  [6][N]              ( 96 B per 5D site)
 //     FP16: uint4   [3][N] + float [N]  ( 52 B per 5D site; __half2 values
 //           normalised by a per-site FP32 scale = max |component|)
+//     double-float: float4 [12][N]      (192 B per 5D site; (re.h, im.h, re.l, im.l))
 //   A full field is [even half][odd half].
 //   cb4 = (x0/2) + (L0/2)*(x1 + L1*(x2 + L2*x3)); parity = (x0+x1+x2+x3) & 1.
 //
@@ -17,6 +18,7 @@
 //     L32  : float2  [9]  (same, FP32)
 //     L32R : float4  [3]  (rows 0,1 of an SU(3) matrix; row 2 rebuilt as
 //                          conj(row0 x row1); phase and -cc_mu/2 at run time)
+//     LDD  : float4  [9]  (as L64, each complex as (re.h, im.h, re.l, im.l))
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
@@ -205,15 +207,16 @@ template <> __device__ __forceinline__ void store_spinor<P64>(void* base, long l
 #pragma unroll
   for (int k = 0; k < 12; ++k) p[n + k * N] = v[k];
 }
-// double-float: float4 (re.h, re.l, im.h, im.l) [12][N]
+// double-float: float4 (re.h, im.h, re.l, im.l) [12][N]: one 16-byte load
+// gives the packed high pair and the packed low pair of a complex number
 template <> __device__ __forceinline__ void load_spinor<PDD>(const void* base, long long N_, long long n_, ddc (&v)[12]) {
   const float4* p = reinterpret_cast<const float4*>(base);
   const unsigned N = (unsigned)N_, n = (unsigned)n_;
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
     const float4 q = __ldg(p + (n + k * N));
-    v[k].x = dd(q.x, q.y);
-    v[k].y = dd(q.z, q.w);
+    v[k].x = dd(q.x, q.z);
+    v[k].y = dd(q.y, q.w);
   }
 }
 template <> __device__ __forceinline__ void store_spinor<PDD>(void* base, long long N_, long long n_, const ddc (&v)[12]) {
@@ -223,7 +226,7 @@ template <> __device__ __forceinline__ void store_spinor<PDD>(void* base, long l
   for (int k = 0; k < 12; ++k) {
     ddc w = v[k];
     nrm<dd>(w);  // memory holds normalised pairs
-    p[n + k * N] = make_float4(w.x.h, w.x.l, w.y.h, w.y.l);
+    p[n + k * N] = make_float4(w.x.h, w.y.h, w.x.l, w.y.l);
   }
 }
 template <> __device__ __forceinline__ void load_spinor<P32>(const void* base, long long N_, long long n_, float2 (&v)[12]) {
@@ -307,8 +310,8 @@ template <> __device__ __forceinline__ void load_link<LDD, dd>(const void* links
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const float4 q = __ldg(b + (o + (unsigned)k * (unsigned)Vh));
-    u[k].x = dd(q.x, q.y);
-    u[k].y = dd(q.z, q.w);
+    u[k].x = dd(q.x, q.z);
+    u[k].y = dd(q.y, q.w);
   }
 }
 template <> __device__ __forceinline__ void load_link<L32, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
@@ -388,8 +391,8 @@ __device__ __forceinline__ void load_spin_dd(const void* base, long long N_, uns
 #pragma unroll
   for (int col = 0; col < 3; ++col) {
     const float4 q = __ldg(p + (n + (unsigned)(3 * k + col) * N));
-    v[col].x = dd(q.x, q.y);
-    v[col].y = dd(q.z, q.w);
+    v[col].x = dd(q.x, q.z);
+    v[col].y = dd(q.y, q.w);
   }
 }
 

@@ -31,6 +31,15 @@
 
 namespace gbf {
 
+// Offset (in 16-byte units) of the double-float accumulators in dynamic
+// shared memory: after the s-matrix tile and the reduction scratch.
+__host__ __device__ inline unsigned dd_acc_offset16(int LK, unsigned bd) {
+  size_t s = 0;
+  if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * 8 + 8;
+  s += 2 * (size_t)bd * 8;
+  return (unsigned)((s + 15) / 16);
+}
+
 template <int P, int LS, int LK, bool LOOP>
 __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MINB_DD : GBF_DSLASH_MINB)) dslash_kernel(const DslashArgs a) {
   using R = typename SpinorT<P>::R;
@@ -52,66 +61,80 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
   for (int k = 0; k < 12; ++k) res[k] = cz<R>();
   int cb = 0;
   if constexpr (P == PDD) {
-   if (active) {
-    // double-float: the same hop with a rolled direction loop (one iteration
-    // is about 1.5k instructions; unrolled eight times the kernel would not
-    // fit the instruction cache)
-    cb = (int)g.fN5.div((unsigned)n);
-    const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
-    const Coord c = cb_coords(g, cb, p);
+    if (active) {
+      // double-float, rolled direction loop (one iteration is about 1.5k
+      // instructions; unrolled eight times the kernel would not fit the
+      // instruction cache).  The 12 accumulators live in shared memory
+      // ([component][thread], 16 B each) during the loop, which frees 48
+      // registers per thread for more resident warps.
+      cb = (int)g.fN5.div((unsigned)n);
+      const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
+      const Coord c = cb_coords(g, cb, p);
+      float4* acc = reinterpret_cast<float4*>(smem_d) + dd_acc_offset16(LK, blockDim.x) + threadIdx.x;
+      const unsigned bs = blockDim.x;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) acc[k * bs] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-    for (int d = 0; d < 8; ++d) {
-      const int mu = d >> 1;
-      const bool fwd = (d & 1) == 0;
-      int y[4];
+      for (int d = 0; d < 8; ++d) {
+        const int mu = d >> 1;
+        const bool fwd = (d & 1) == 0;
+        int y[4];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int xm = c.x[m], Lm = g.L[m];
-        y[m] = (m != mu) ? xm : fwd ? (xm == Lm - 1 ? 0 : xm + 1) : (xm == 0 ? Lm - 1 : xm - 1);
+        for (int m = 0; m < 4; ++m) {
+          const int xm = c.x[m], Lm = g.L[m];
+          y[m] = (m != mu) ? xm : fwd ? (xm == Lm - 1 ? 0 : xm + 1) : (xm == 0 ? Lm - 1 : xm - 1);
+        }
+        const int ycb = cb_index(g, y);
+        const unsigned site = (unsigned)ycb * (unsigned)g.N5 + i5;
+        const float s = fwd ? a.sgn : -a.sgn;
+        cplx<dd> h[2][3];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          cplx<dd> up[3], lo[3];
+          load_spin_dd(a.in, g.N, site, r, up);
+          load_spin_dd(a.in, g.N, site, gperm(mu, r), lo);
+          const int cr = gcoef(mu, r);
+#pragma unroll
+          for (int col = 0; col < 3; ++col) h[r][col] = coefmadd_rt(cr, s, lo[col], up[col]);
+        }
+        cplx<dd> u[9];
+        load_link<LDD, dd>(a.links, g.Vh, fwd ? p : q, mu, fwd ? cb : ycb, u);
+        cplx<dd> uh[2][3];
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            cplx<dd> t = cz<dd>();
+#pragma unroll
+            for (int j = 0; j < 3; ++j) t = fwd ? cmadd<dd>(t, u[3 * i + j], h[r][j]) : cmaddc<dd>(t, u[3 * j + i], h[r][j]);
+            uh[r][i] = t;
+          }
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            float4& m = acc[(3 * r + i) * bs];
+            const cplx<dd> v = add<dd>(mk<dd>(dd(m.x, m.z), dd(m.y, m.w)), uh[r][i]);
+            m = make_float4(v.x.h, v.y.h, v.x.l, v.y.l);
+          }
+#pragma unroll
+        for (int r = 2; r < 4; ++r) {
+          const bool first = gperm(mu, r) == 0;
+          const int cr = gcoef(mu, r);
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            float4& m = acc[(3 * r + i) * bs];
+            const cplx<dd> v = coefmadd_rt(cr, s, first ? uh[0][i] : uh[1][i], mk<dd>(dd(m.x, m.z), dd(m.y, m.w)));
+            m = make_float4(v.x.h, v.y.h, v.x.l, v.y.l);
+          }
+        }
       }
-      const int ycb = cb_index(g, y);
-      const unsigned site = (unsigned)ycb * (unsigned)g.N5 + i5;
-      const float s = fwd ? a.sgn : -a.sgn;
-      cplx<dd> h[2][3];
 #pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        cplx<dd> up[3], lo[3];
-        load_spin_dd(a.in, g.N, site, r, up);
-        load_spin_dd(a.in, g.N, site, gperm(mu, r), lo);
-        const int cr = gcoef(mu, r);
-#pragma unroll
-        for (int col = 0; col < 3; ++col) h[r][col] = coefmadd_rt(cr, s, lo[col], up[col]);
-      }
-      cplx<dd> u[9];
-      load_link<LDD, dd>(a.links, g.Vh, fwd ? p : q, mu, fwd ? cb : ycb, u);
-      cplx<dd> uh[2][3];
-#pragma unroll
-      for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          cplx<dd> acc = cz<dd>();
-#pragma unroll
-          for (int j = 0; j < 3; ++j) acc = fwd ? cmadd<dd>(acc, u[3 * i + j], h[r][j]) : cmaddc<dd>(acc, u[3 * j + i], h[r][j]);
-          uh[r][i] = acc;
-        }
-#pragma unroll
-      for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          res[3 * r + i] = add<dd>(res[3 * r + i], uh[r][i]);
-        }
-#pragma unroll
-      for (int r = 2; r < 4; ++r) {
-        const bool first = gperm(mu, r) == 0;
-        const int cr = gcoef(mu, r);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          cplx<dd>& t = res[3 * r + i];
-          t = coefmadd_rt(cr, s, first ? uh[0][i] : uh[1][i], t);
-        }
+      for (int k = 0; k < 12; ++k) {
+        const float4 m = acc[k * bs];
+        res[k] = mk<dd>(dd(m.x, m.z), dd(m.y, m.w));
       }
     }
-   }
   } else if (active) {
     cb = (int)g.fN5.div((unsigned)n);
     const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
@@ -183,7 +206,12 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
       smat_apply_block<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res, true);
     }
   } else if (active && a.l1.kind != LOC_NONE) {
-    local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
+    if constexpr (P == PDD) {
+      if (a.l1.kind == LOC_CLOVER) clover_apply_dd_lowreg(a.l1.clov[p], g.Vh, cb, res);
+      else local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
+    } else {
+      local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
+    }
   }
   if (active) {
     if (a.c1 != 1.0) {
@@ -197,7 +225,14 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
     if (a.X) {
       V xv[12];
       load_spinor<P>(a.X, g.N, n, xv);
-      if (LK != LOC_SMAT && a.l2.kind != LOC_NONE) local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+      if (LK != LOC_SMAT && a.l2.kind != LOC_NONE) {
+        if constexpr (P == PDD) {
+          if (a.l2.kind == LOC_CLOVER) clover_apply_dd_lowreg(a.l2.clov[p], g.Vh, cb, xv);
+          else local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+        } else {
+          local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+        }
+      }
       const R c2 = (R)a.c2;
 #pragma unroll
       for (int k = 0; k < 12; ++k) res[k] = mk<R>(fma(c2, xv[k].x, res[k].x), fma(c2, xv[k].y, res[k].y));
@@ -262,6 +297,7 @@ size_t dslash_smem_bytes(int P, int LK, int bd) {
   size_t s = 0;
   if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
   s += 2 * (size_t)bd * 8;
+  if (P == PDD) s = 16 * (size_t)dd_acc_offset16(LK, bd) + 12 * 16 * (size_t)bd;  // + accumulators
   return s;
 }
 

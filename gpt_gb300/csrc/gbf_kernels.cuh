@@ -2,7 +2,6 @@
 // site-local operators (clover, s-matrix), the deterministic block reduction
 // and its last-block finalisation, and the CG scalar updates.
 #pragma once
-#include <type_traits>
 #include "gbf_common.cuh"
 
 namespace gbf {
@@ -44,55 +43,100 @@ template <> struct CloverLoad<float> {
     }
   }
 };
-// double-float: the FP64 layout with each double2 stored as float4 (x.h, x.l, y.h, y.l)
-template <> struct CloverLoad<dd> {
-  static __device__ __forceinline__ void block(const void* base, int Vh, int cb, int b, dd (&c)[36]) {
-    const float4* p = reinterpret_cast<const float4*>(base) + ((unsigned)cb + 18u * (unsigned)b * (unsigned)Vh);
-#pragma unroll
-    for (int k = 0; k < 18; ++k) {
-      const float4 q = __ldg(p + (unsigned)k * (unsigned)Vh);
-      c[2 * k] = dd(q.x, q.y);
-      c[2 * k + 1] = dd(q.z, q.w);
-    }
-  }
-};
-
 // off-diagonal index of (i, j), i > j
 __host__ __device__ constexpr int tri(int i, int j) { return i * (i - 1) / 2 + j; }
 
-// The double-float variant keeps the two chiral blocks in a rolled loop (the
-// block is selected into w and written back by predicated moves): its fully
-// unrolled code would not fit the instruction cache.
 template <typename R>
 __device__ __forceinline__ void clover_apply(const void* base, int Vh, int cb, cplx<R> (&v)[12]) {
-  constexpr bool kRoll = std::is_same<R, dd>::value;
-#pragma unroll(kRoll ? 1 : 2)
+#pragma unroll
   for (int b = 0; b < 2; ++b) {
     R c[36];
     CloverLoad<R>::block(base, Vh, cb, b, c);
-    cplx<R> w[6], o[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) w[i] = b ? v[6 + i] : v[i];
+    cplx<R> o[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-      cplx<R> acc = scl<R>(c[i], w[i]);
+      cplx<R> acc = scl<R>(c[i], v[6 * b + i]);
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
         if (j < i) {
           const int t = tri(i, j);
-          acc = cmadd<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), w[j]);
+          acc = cmadd<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), v[6 * b + j]);
         } else if (j > i) {
           const int t = tri(j, i);
-          acc = cmaddc<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), w[j]);
+          acc = cmaddc<R>(acc, mk<R>(c[6 + 2 * t], c[6 + 2 * t + 1]), v[6 * b + j]);
         }
       }
       o[i] = acc;
     }
 #pragma unroll
+    for (int i = 0; i < 6; ++i) v[6 * b + i] = o[i];
+  }
+}
+
+// Double-float clover for site-local kernels: all loads of a block issued
+// together, the two blocks in a rolled loop (the block is selected into w and
+// written back by predicated moves) to keep the code in the instruction cache.
+template <>
+__device__ __forceinline__ void clover_apply<dd>(const void* base, int Vh, int cb, ddc (&v)[12]) {
+  const float4* p0 = reinterpret_cast<const float4*>(base) + cb;
+#pragma unroll 1
+  for (int b = 0; b < 2; ++b) {
+    const float4* p = p0 + 18u * (unsigned)b * (unsigned)Vh;
+    float4 q[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) q[k] = __ldg(p + (unsigned)k * (unsigned)Vh);
+    ddc w[6], o[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) w[i] = b ? v[6 + i] : v[i];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      o[2 * k] = scl<dd>(dd(q[k].x, q[k].z), w[2 * k]);
+      o[2 * k + 1] = scl<dd>(dd(q[k].y, q[k].w), w[2 * k + 1]);
+    }
+#pragma unroll
+    for (int i = 1; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < i; ++j) {
+        const float4 e = q[3 + tri(i, j)];
+        const ddc cij = mk<dd>(dd(e.x, e.z), dd(e.y, e.w));
+        o[i] = cmadd<dd>(o[i], cij, w[j]);
+        o[j] = cmaddc<dd>(o[j], cij, w[i]);
+      }
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
       if (b) v[6 + i] = o[i];
       else v[i] = o[i];
     }
+  }
+}
+
+// Double-float clover for the register-capped hopping kernel: entry by entry
+// (each off-diagonal entry is loaded right before its two uses, row i and,
+// conjugated, row j), so that no more than one entry is live.
+__device__ __forceinline__ void clover_apply_dd_lowreg(const void* base, int Vh, int cb, ddc (&v)[12]) {
+  const float4* p0 = reinterpret_cast<const float4*>(base) + cb;
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    const float4* p = p0 + 18u * (unsigned)b * (unsigned)Vh;
+    ddc* w = v + 6 * b;
+    ddc o[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float4 q = __ldg(p + (unsigned)k * (unsigned)Vh);
+      o[2 * k] = scl<dd>(dd(q.x, q.z), w[2 * k]);
+      o[2 * k + 1] = scl<dd>(dd(q.y, q.w), w[2 * k + 1]);
+    }
+#pragma unroll
+    for (int i = 1; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < i; ++j) {
+        const float4 q = __ldg(p + (unsigned)(3 + tri(i, j)) * (unsigned)Vh);
+        const ddc cij = mk<dd>(dd(q.x, q.z), dd(q.y, q.w));
+        o[i] = cmadd<dd>(o[i], cij, w[j]);
+        o[j] = cmaddc<dd>(o[j], cij, w[i]);
+      }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) w[i] = o[i];
   }
 }
 

@@ -96,7 +96,7 @@ cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double cs
 // FP64 clover storage (double2 [2*nrows32][Vh]) -> FP32 (float4 [nrows32][Vh]);
 // nrows32 is a row count (18 per parity block), not an element count
 cudaError_t launch_clover_narrow(const void* src64, void* dst32, long long nrows32, int Vh, cudaStream_t st);
-// the same from double-float storage (float4 (x.h, x.l, y.h, y.l) per double2)
+// the same from double-float storage (float4 (x.h, y.h, x.l, y.l) per double2)
 cudaError_t launch_clover_narrow_dd(const void* srcdd, void* dst32, long long nrows32, int Vh, cudaStream_t st);
 // FP64 complex array -> double-float (float4 per complex), n_complex elements
 cudaError_t launch_split_dd(const void* src64, void* dst, long long n_complex, cudaStream_t st);

@@ -405,7 +405,7 @@ __global__ void pack_links_kernel(Geo g, const double2* U, void* links, LamPh la
     float4* b = reinterpret_cast<float4*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
     for (int k = 0; k < 9; ++k) {
       const dd re(u[k].x), im(u[k].y);
-      b[(size_t)k * g.Vh] = make_float4(re.h, re.l, im.h, im.l);
+      b[(size_t)k * g.Vh] = make_float4(re.h, im.h, re.l, im.l);
     }
   } else {
     float2* b = reinterpret_cast<float2*>(links) + (size_t)(par * 4 + mu) * 9 * g.Vh + cb;
@@ -638,13 +638,13 @@ cudaError_t launch_clover_narrow(const void* src64, void* dst32, long long nrows
   return cudaGetLastError();
 }
 
-// double-float source: each double2 of the FP64 layout is a float4 (x.h, x.l, y.h, y.l)
+// double-float source: each double2 of the FP64 layout is a float4 (x.h, y.h, x.l, y.l)
 __global__ void clover_narrow_dd_kernel(const float4* src, float4* dst, long long nrows32, int Vh) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrows32 * Vh) return;
   const long long row = t / Vh, cb = t - row * Vh;
   const float4 a = src[(2 * row) * Vh + cb], b = src[(2 * row + 1) * Vh + cb];
-  dst[row * Vh + cb] = make_float4(__fadd_rn(a.x, a.y), __fadd_rn(a.z, a.w), __fadd_rn(b.x, b.y), __fadd_rn(b.z, b.w));
+  dst[row * Vh + cb] = make_float4(__fadd_rn(a.x, a.z), __fadd_rn(a.y, a.w), __fadd_rn(b.x, b.z), __fadd_rn(b.y, b.w));
 }
 
 cudaError_t launch_clover_narrow_dd(const void* srcdd, void* dst32, long long nrows32, int Vh, cudaStream_t st) {
@@ -658,7 +658,7 @@ __global__ void split_dd_kernel(const double2* src, float4* dst, long long n) {
   if (t >= n) return;
   const double2 a = src[t];
   const dd x(a.x), y(a.y);
-  dst[t] = make_float4(x.h, x.l, y.h, y.l);
+  dst[t] = make_float4(x.h, y.h, x.l, y.l);
 }
 
 cudaError_t launch_split_dd(const void* src64, void* dst, long long n_complex, cudaStream_t st) {
