@@ -44,7 +44,7 @@ CFG = dict(dims=[32, 32, 32, 32], gauge_eps=0.3, gauge_seed=2024, src_seed=7, ma
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbf", choices=["gbf", "reference"])
     ap.add_argument("--dims", type=str, default=None, help="override lattice, e.g. 16,16,16,16 (tests only)")

@@ -16,6 +16,9 @@
 // Roofline: HBM-bound in FP32/FP16 (per output site: 8 neighbour spinors that
 // the L2 mostly serves once, 8 links, 1 output); FP64 is bound by the FP64
 // pipe on GB300 (about 1.2 TFLOP/s measured).
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "gbf_launch.cuh"
 
 // resident blocks of 256 threads per SM requested for the FP32/FP16 variants
@@ -262,17 +265,44 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
 // ---------------------------------------------------------------------------
 // host-side launcher
 // ---------------------------------------------------------------------------
-// Grid of a reducing launch: enough blocks to fill the GPU, few enough that
-// the last block's pass over the [block][rhs] partials stays short.
-long long reduce_grid(long long ntiles, int nrhs) {
+static int sm_count() {
   static const int sms = [] {
     int d = 0, c = 152;
     if (cudaGetDevice(&d) == cudaSuccess) cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, d);
     return c;
   }();
-  long long cap = 4LL * sms;
-  const long long by_partials = 4096LL / (nrhs > 0 ? nrhs : 1);
-  if (by_partials > cap) cap = by_partials;
+  return sms;
+}
+
+// Blocks of `kernel` resident per SM at block size bd and dynamic shared
+// memory smem (also raises the kernel's dynamic shared-memory limit when smem
+// exceeds the default 48 KB); cached per (kernel, bd, smem).
+int resident_blocks(const void* kernel, int bd, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, size_t>, int> cache;
+  const auto key = std::make_tuple(kernel, bd, smem);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, bd, smem) != cudaSuccess || nb < 1) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  cache[key] = nb;
+  return nb;
+}
+
+// Grid of a reducing launch: one full wave of resident blocks (every block
+// then loops over an equal share of the tiles, with no partial last wave),
+// and no more blocks than tiles.  The [block][rhs] partials stay few.
+// min_partials > 0 allows more blocks, up to min_partials / nrhs, before the
+// grid is capped (for kernels whose looping variant is slower).
+long long reduce_grid(long long ntiles, int nrhs, int resident, long long min_partials) {
+  long long cap = (long long)sm_count() * (resident > 0 ? resident : 1);
+  const long long alt = min_partials / (nrhs > 0 ? nrhs : 1);
+  if (alt > cap) cap = alt;
   return ntiles < cap ? ntiles : cap;
 }
 
@@ -301,18 +331,19 @@ size_t dslash_smem_bytes(int P, int LK, int bd) {
   return s;
 }
 
+// The double-float kernel's looping variant needs more registers (spills):
+// its reducing launches keep one tile per block up to 4096 blocks.
+static long long dslash_min_partials(int P) { return P == PDD ? 4096 : 0; }
+
 template <int P, int LS, int LK, bool LOOP>
 static cudaError_t launch_tl(const DslashArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
-  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
   const size_t sm = dslash_smem_bytes(P, LK, bd);
   auto k = dslash_kernel<P, LS, LK, LOOP>;
-  if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-  }
+  const int res = resident_blocks((const void*)k, bd, sm);
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs, res, dslash_min_partials(P)) : ntiles;
   k<<<(unsigned)nb, bd, sm, st>>>(a);
   return cudaGetLastError();
 }
@@ -322,7 +353,8 @@ static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
-  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs) < ntiles;
+  const int res = resident_blocks((const void*)dslash_kernel<P, LS, LK, true>, bd, dslash_smem_bytes(P, LK, bd));
+  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs, res, dslash_min_partials(P)) < ntiles;
   return loop ? launch_tl<P, LS, LK, true>(a, st) : launch_tl<P, LS, LK, false>(a, st);
 }
 

@@ -26,7 +26,8 @@ cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st);
 int block_size_for(int N5, int LK);
 // requested block size if valid for N5, else the default
 int pick_bd(int requested, int N5);
-long long reduce_grid(long long ntiles, int nrhs);
+long long reduce_grid(long long ntiles, int nrhs, int resident, long long min_partials = 0);
+int resident_blocks(const void* kernel, int bd, size_t smem);
 long long dslash_blocks(const Geo& g, int LK);
 
 // Site-local kernel on one parity (gbf_local.cu):

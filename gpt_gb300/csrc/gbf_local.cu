@@ -104,13 +104,10 @@ static cudaError_t launch_local_tl(const LocalArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
-  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
   const size_t sm = local_smem(P, LK, bd);
   auto k = local_kernel<P, LK, LOOP>;
-  if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-  }
+  const int res = resident_blocks((const void*)k, bd, sm);
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs, res) : ntiles;
   k<<<(unsigned)nb, bd, sm, st>>>(a);
   return cudaGetLastError();
 }
@@ -120,7 +117,8 @@ static cudaError_t launch_local_t(const LocalArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
-  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs) < ntiles;
+  const int res = resident_blocks((const void*)local_kernel<P, LK, true>, bd, local_smem(P, LK, bd));
+  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs, res) < ntiles;
   return loop ? launch_local_tl<P, LK, true>(a, st) : launch_local_tl<P, LK, false>(a, st);
 }
 
@@ -170,13 +168,17 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
 cudaError_t launch_cg_update(int P, const CGUpdateArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
-  const long long nb = reduce_grid((a.g.N + bd - 1) / bd, a.g.nrhs);
   const size_t sm = 2 * (size_t)bd * 8;
+  const void* k = P == P64 ? (const void*)cg_update_kernel<P64>
+                : P == P32 ? (const void*)cg_update_kernel<P32>
+                : P == P16 ? (const void*)cg_update_kernel<P16>
+                : P == PDD ? (const void*)cg_update_kernel<PDD> : nullptr;
+  if (!k) return cudaErrorInvalidValue;
+  const long long nb = reduce_grid((a.g.N + bd - 1) / bd, a.g.nrhs, resident_blocks(k, bd, sm));
   if (P == P64) cg_update_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P32) cg_update_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P16) cg_update_kernel<P16><<<(unsigned)nb, bd, sm, st>>>(a);
-  else if (P == PDD) cg_update_kernel<PDD><<<(unsigned)nb, bd, sm, st>>>(a);
-  else return cudaErrorInvalidValue;
+  else cg_update_kernel<PDD><<<(unsigned)nb, bd, sm, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -224,8 +226,13 @@ cudaError_t launch_blas(int P, const BlasArgs& a, cudaStream_t st) {
   const int bd = block_size_for(a.g.N5, LOC_NONE);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
-  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs) : ntiles;
   const size_t sm = 2 * (size_t)bd * 8;
+  const void* k = P == P64 ? (const void*)blas_kernel<P64>
+                : P == P32 ? (const void*)blas_kernel<P32>
+                : P == P16 ? (const void*)blas_kernel<P16>
+                : P == PDD ? (const void*)blas_kernel<PDD> : nullptr;
+  if (!k) return cudaErrorInvalidValue;
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs, resident_blocks(k, bd, sm)) : ntiles;
   if (P == P64) blas_kernel<P64><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P32) blas_kernel<P32><<<(unsigned)nb, bd, sm, st>>>(a);
   else if (P == P16) blas_kernel<P16><<<(unsigned)nb, bd, sm, st>>>(a);
