@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=40, help="c5: number of requests")
     ap.add_argument("--inner", default="single", choices=["single", "half"], help="c3/c4 inner precision")
     ap.add_argument("--rhs-group", type=int, default=0, help="c4: right-hand sides solved together (0: auto)")
+    ap.add_argument("--solver", default="cg", choices=["cg", "block_cg"],
+                    help="c3/c4 inner solver: independent CG per packed rhs, or block CG over them")
     return ap.parse_args()
 
 
@@ -146,7 +148,8 @@ def run_mobius_config(args, which):
     op = g.qcd.fermion.mobius(U, params)
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
-    inner_cg = inv.cg({"eps": inner_tol, "maxiter": 50000, "iterations_per_graph": 16})
+    inner_kind = inv.block_cg if args.solver == "block_cg" else inv.cg
+    inner_cg = inner_kind({"eps": inner_tol, "maxiter": 50000, "iterations_per_graph": 16})
     dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inner_cg), inner_prec, g.double),
                                eps=tol, maxiter=200)
     solver = dc(op)
@@ -210,7 +213,7 @@ def run_mobius_config(args, which):
     value = nsrc * args.steps / (total_ms / 1000.0)
     cfg = {"workload": f"mobius {'x'.join(map(str, dims))} Ls {Ls} b 1.5 c 0.5 M5 1.8 mass {mass} gauge eps {geps}, "
                        f"{nsrc} {'point' if which == 'c3' else 'gaussian'} sources in {ngroups} packed group(s) of {group}, "
-                       f"propagator Export*solve*Import, defect correction ({args.inner} inner, tol {inner_tol}) "
+                       f"propagator Export*solve*Import, defect correction ({args.inner} inner {args.solver}, tol {inner_tol}) "
                        f"to true residual {tol}", "lattice": dims, "Ls": Ls,
            "l2_policy": "inputs larger than L2; no flush", "parallelism": "replicas"}
     line = _common_line(METRIC, value, "solves/s", args, 1, total_ms, cfg, f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",

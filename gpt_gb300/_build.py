@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbferm.so")
-SOURCES = ["gbf_dslash.cu", "gbf_local.cu", "gbf_api.cu", "gbf_noalloc.cu", "gbf_random.cu"]
+SOURCES = ["gbf_dslash.cu", "gbf_local.cu", "gbf_api.cu", "gbf_noalloc.cu", "gbf_random.cu", "gbf_block.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -36,6 +36,21 @@ class cg:
         raise NotImplementedError("cg runs on the device through preconditioned(eo2_ne(), cg(...))")
 
 
+class block_cg(cg):
+    """gpt.algorithms.inverter.block_cg(eps, maxiter) (block_cg.py:36-149):
+    the packed right-hand sides of an n_rhs operator share one Krylov space;
+    converged when max_b |r_b|^2 / |b_b|^2 <= eps^2 as recorded by the block
+    recursion.  Runs on the device through preconditioned(eo2_ne(), ...)."""
+
+    def modified(self, **params):
+        d = dict(eps=self.eps, maxiter=self.maxiter, fail_if_not_converged=self.fail_if_not_converged)
+        d.update(params)
+        return block_cg(d)
+
+    def __call__(self, mat):
+        raise NotImplementedError("block_cg runs on the device through preconditioned(eo2_ne(), block_cg(...))")
+
+
 class preconditioned:
     """M^-1 = L Mpc^-1 R + S (preconditioned.py:28-54)."""
 
@@ -45,15 +60,17 @@ class preconditioned:
 
     def __call__(self, op):
         if not isinstance(self.preconditioner, _fermion.preconditioner.eo2_ne) or not isinstance(self.inverter, cg):
-            raise NotImplementedError("the device path implements preconditioned(eo2_ne(), cg(...))")
+            raise NotImplementedError("the device path implements preconditioned(eo2_ne(), cg(...) or block_cg(...))")
         if not isinstance(op, _fermion.fermion_operator):
             raise TypeError("expected a native fermion operator")
         if op.daggered:
             raise NotImplementedError("solves with the daggered operator are not on this path")
         inv = self.inverter
 
+        solve = op._solve_eo2ne_block_cg if isinstance(inv, block_cg) else op._solve_eo2ne_cg
+
         def mat(dst, src):
-            r = op._solve_eo2ne_cg(dst, src, inv.eps, inv.maxiter, inv.iterations_per_graph)
+            r = solve(dst, src, inv.eps, inv.maxiter, inv.iterations_per_graph)
             inv.last = r
             inv.history = [None] * r.iterations
             inv.total_iterations += r.iterations

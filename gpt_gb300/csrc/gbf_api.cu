@@ -11,7 +11,9 @@
 //                                         normal_equation.py:35-65, inverter/cg.py:24-117
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <cmath>
+#include <complex>
 #include <string>
 #include <vector>
 #include <stdexcept>
@@ -103,6 +105,12 @@ struct gbf_op {
   // block sizes chosen by gbf_tune (0: default): hop with a per-thread
   // epilogue, hop with the s-matrix epilogue, site-local kernel, CG update
   int tuned_bd[4] = {0, 0, 0, 0};
+  // block CG workspace: Gram partials [max_blocks][k*k], device results and
+  // coefficient matrices (k*k Gram + 4 x k*k), pinned host mirror
+  double2* blk_partial = nullptr;
+  double2* blk_dev = nullptr;
+  double2* blk_host = nullptr;
+  long long blk_max_blocks = 0;
 
   size_t half() const { return (size_t)half_bytes(prec, g.N); }
   // workspace half field i; halves 2k and 2k+1 are one contiguous full field,
@@ -348,6 +356,9 @@ void free_op(gbf_op* op) {
   cudaFree(op->smat);
   for (void* m : op->pair_mem) cudaFree(m);
   cudaFree(op->partial);
+  cudaFree(op->blk_partial);
+  cudaFree(op->blk_dev);
+  if (op->blk_host) cudaFreeHost(op->blk_host);
   cudaFree(op->counter);
   cudaFree(op->st);
   cudaFree(op->errbits);
@@ -1046,3 +1057,252 @@ int gbf_set_tuning(gbf_op* op, const int* bd) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// block CG (lib/gpt/algorithms/inverter/block_cg.py:36-149, after Grid's
+// BlockConjugateGradient with a Cholesky QR): the k = n_rhs packed right-hand
+// sides of the eo2_ne normal equations share one Krylov space.  Vectors and
+// Gram matrices live on the device; the k x k algebra (inverse, Cholesky)
+// runs on the host in complex128, as in the reference, with one Gram read
+// back per half iteration.
+// ---------------------------------------------------------------------------
+namespace {
+
+using zc = std::complex<double>;
+using zmat = std::vector<zc>;  // k x k, row-major
+
+zmat zmul(int k, const zmat& a, const zmat& b) {
+  zmat c((size_t)k * k, zc(0.0, 0.0));
+  for (int i = 0; i < k; ++i)
+    for (int l = 0; l < k; ++l) {
+      const zc ail = a[(size_t)i * k + l];
+      for (int j = 0; j < k; ++j) c[(size_t)i * k + j] += ail * b[(size_t)l * k + j];
+    }
+  return c;
+}
+zmat zadj(int k, const zmat& a) {
+  zmat c((size_t)k * k);
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < k; ++j) c[(size_t)j * k + i] = std::conj(a[(size_t)i * k + j]);
+  return c;
+}
+// Cholesky of the Hermitian part of A: A = L L^H, L lower; false if A is not
+// positive definite or numerically rank deficient (a pivot below 1e-13 of
+// its diagonal entry: linearly dependent block vectors)
+bool zcholesky(int k, const zmat& A, zmat& L) {
+  L.assign((size_t)k * k, zc(0.0, 0.0));
+  for (int j = 0; j < k; ++j) {
+    const double ajj = A[(size_t)j * k + j].real();
+    double d = ajj;
+    for (int l = 0; l < j; ++l) d -= std::norm(L[(size_t)j * k + l]);
+    if (!(d > 1e-13 * ajj) || !std::isfinite(d)) return false;
+    const double ljj = std::sqrt(d);
+    L[(size_t)j * k + j] = ljj;
+    for (int i = j + 1; i < k; ++i) {
+      zc v = 0.5 * (A[(size_t)i * k + j] + std::conj(A[(size_t)j * k + i]));
+      for (int l = 0; l < j; ++l) v -= L[(size_t)i * k + l] * std::conj(L[(size_t)j * k + l]);
+      L[(size_t)i * k + j] = v / ljj;
+    }
+  }
+  return true;
+}
+// inverse of an upper-triangular U
+zmat zinv_upper(int k, const zmat& U) {
+  zmat X((size_t)k * k, zc(0.0, 0.0));
+  for (int c = 0; c < k; ++c) {
+    for (int i = c; i >= 0; --i) {
+      zc v = (i == c) ? zc(1.0, 0.0) : zc(0.0, 0.0);
+      for (int l = i + 1; l <= c; ++l) v -= U[(size_t)i * k + l] * X[(size_t)l * k + c];
+      X[(size_t)i * k + c] = v / U[(size_t)i * k + i];
+    }
+  }
+  return X;
+}
+// general inverse, Gauss-Jordan with partial pivoting; false if singular
+bool zinv(int k, zmat A, zmat& X) {
+  X.assign((size_t)k * k, zc(0.0, 0.0));
+  for (int i = 0; i < k; ++i) X[(size_t)i * k + i] = 1.0;
+  for (int c = 0; c < k; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < k; ++r)
+      if (std::abs(A[(size_t)r * k + c]) > std::abs(A[(size_t)piv * k + c])) piv = r;
+    if (std::abs(A[(size_t)piv * k + c]) == 0.0 || !std::isfinite(std::abs(A[(size_t)piv * k + c]))) return false;
+    for (int l = 0; l < k; ++l) {
+      std::swap(A[(size_t)c * k + l], A[(size_t)piv * k + l]);
+      std::swap(X[(size_t)c * k + l], X[(size_t)piv * k + l]);
+    }
+    const zc d = 1.0 / A[(size_t)c * k + c];
+    for (int l = 0; l < k; ++l) {
+      A[(size_t)c * k + l] *= d;
+      X[(size_t)c * k + l] *= d;
+    }
+    for (int r = 0; r < k; ++r) {
+      if (r == c) continue;
+      const zc f = A[(size_t)r * k + c];
+      if (f == zc(0.0, 0.0)) continue;
+      for (int l = 0; l < k; ++l) {
+        A[(size_t)r * k + l] -= f * A[(size_t)c * k + l];
+        X[(size_t)r * k + l] -= f * X[(size_t)c * k + l];
+      }
+    }
+  }
+  return true;
+}
+
+void ensure_block_ws(gbf_op* op) {
+  if (op->blk_partial) return;
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int k = op->g.nrhs;
+  op->blk_max_blocks = (long long)sms * 32;
+  op->blk_partial = (double2*)dmalloc((size_t)op->blk_max_blocks * k * k * sizeof(double2));
+  op->blk_dev = (double2*)dmalloc((size_t)5 * k * k * sizeof(double2));
+  CK(cudaMallocHost(&op->blk_host, (size_t)5 * k * k * sizeof(double2)));
+}
+
+// Z = Mpc^+ Mpc D on the odd sites (the CG iteration's kernel sequence)
+void apply_ne(gbf_op* op, cudaStream_t s, const void* in, void* out) {
+  const int D = GBF_ODD, C = GBF_EVEN;
+  void *t = op->T(0), *z = op->T(1), *w = op->T(2), *u = op->T(3);
+  op->local(s, D, in, t, op->G());
+  op->dslash(s, C, false, t, z, op->G());
+  op->dslash(s, D, false, z, w, op->none(), -1.0, in, 1.0);
+  op->dslash(s, C, true, w, u, op->Gdag());
+  op->dslash(s, D, true, u, out, op->Gdag(), -1.0, w, 1.0);
+}
+
+// Gram matrix <A_i, B_j> of two packed half fields, read back (synchronises s)
+zmat gram(gbf_op* op, cudaStream_t s, const void* A, const void* B) {
+  const int k = op->g.nrhs;
+  CK(launch_gram(op->prec, op->g, A, B, op->blk_partial, op->blk_max_blocks, op->counter, op->blk_dev, s));
+  count_launch();
+  CK(cudaMemcpyAsync(op->blk_host, op->blk_dev, (size_t)k * k * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  zmat m((size_t)k * k);
+  for (int q = 0; q < k * k; ++q) m[q] = zc(op->blk_host[q].x, op->blk_host[q].y);
+  return m;
+}
+
+double2* upload(gbf_op* op, cudaStream_t s, int slot, const zmat& W) {
+  const int k = op->g.nrhs;
+  double2* h = op->blk_host + (size_t)slot * k * k;
+  for (int q = 0; q < k * k; ++q) h[q] = make_double2(W[q].real(), W[q].imag());
+  double2* d = op->blk_dev + (size_t)slot * k * k;
+  CK(cudaMemcpyAsync(d, h, (size_t)k * k * sizeof(double2), cudaMemcpyHostToDevice, s));
+  return d;
+}
+
+// out1 = b1 Y1 + X1 W1 ; out2 = b2 Y2 + c out1 + X2 W2 (coefficient slots 1, 2 or 3, 4)
+void lincomb2(gbf_op* op, cudaStream_t s, int slot, void* out1, const void* Y1, double b1, const void* X1, const zmat& W1,
+              void* out2, const void* Y2, double b2, double c, const void* X2, const zmat& W2) {
+  double2* d1 = upload(op, s, slot, W1);
+  double2* d2 = upload(op, s, slot + 1, W2);
+  CK(launch_lincomb2(op->prec, op->g, out1, Y1, b1, X1, d1, out2, Y2, b2, c, X2, d2, s));
+  count_launch();
+}
+
+// out = beta Y + X W with W uploaded into coefficient slot `slot` (1..4)
+void lincomb(gbf_op* op, cudaStream_t s, int slot, void* out, const void* Y, double beta, const void* X, const zmat& W) {
+  const int k = op->g.nrhs;
+  double2* h = op->blk_host + (size_t)slot * k * k;
+  for (int q = 0; q < k * k; ++q) h[q] = make_double2(W[q].real(), W[q].imag());
+  double2* d = op->blk_dev + (size_t)slot * k * k;
+  CK(cudaMemcpyAsync(d, h, (size_t)k * k * sizeof(double2), cudaMemcpyHostToDevice, s));
+  CK(launch_lincomb(op->prec, op->g, out, Y, beta, X, d, s));
+  count_launch();
+}
+
+}  // namespace
+
+extern "C" int gbf_solve_eo2ne_block_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* prm,
+                                        gbf_cg_result* res, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !x || !prm) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    ensure_ws(op);
+    ensure_block_ws(op);
+    for (int i = 0; i < 12; ++i) op->T(i);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int k = op->g.nrhs;
+    const int D = GBF_ODD, C = GBF_EVEN;
+    const size_t h = op->half();
+    const void* srcC = (const char*)src + C * h;
+    const void* srcD = (const char*)src + D * h;
+    void* xC = (char*)x + C * h;
+    void* xD = (char*)x + D * h;
+    void *Dv = op->T(4), *B = op->T(5), *Z = op->T(6), *X = op->T(7), *s1 = op->T(8), *tC = op->T(9);
+    void *Q = op->T(10), *tmp = op->T(11), *u = op->T(3);
+    // ---- prepare B = Mpc^+ (src_D - Dhop G_C src_C), |B_b|^2 ----
+    op->local(s, C, srcC, tC, op->G());
+    op->dslash(s, D, false, tC, s1, op->none(), -1.0, srcD, 1.0);
+    op->dslash(s, C, true, s1, u, op->Gdag());
+    op->dslash(s, D, true, u, B, op->Gdag(), -1.0, s1, 1.0, op->none(), 2, nullptr, FIN_STORE);
+    double ssq[kMaxRhs];
+    read_last(op, s, ssq, nullptr);
+    CK(cudaMemsetAsync(X, 0, h, s));
+    int iters = 0, converged = 0, breakdown = 0;
+    std::vector<double> rel(k, 0.0);
+    double total = 0.0;
+    for (int b = 0; b < k; ++b) total += ssq[b];
+    if (total > 0.0) {
+      // QR of R = B (X = 0): Q C = B, D = Q
+      zmat L, Cm;
+      if (!zcholesky(k, gram(op, s, B, B), L)) {
+        breakdown = 1;
+      } else {
+        Cm = zadj(k, L);
+        lincomb(op, s, 1, Q, nullptr, 0.0, B, zinv_upper(k, Cm));
+        CK(cudaMemcpyAsync(Dv, Q, h, cudaMemcpyDeviceToDevice, s));
+        void* Dn = s1;  // free until the reconstruction
+        for (int it = 0; it < prm->maxiter; ++it) {
+          apply_ne(op, s, Dv, Z);
+          zmat M;
+          if (!zinv(k, gram(op, s, Dv, Z), M)) {
+            breakdown = 1;
+            break;
+          }
+          // X += D (M C) ; tmp = Q - Z M
+          zmat mM = M;
+          for (auto& v : mM) v = -v;
+          lincomb2(op, s, 1, X, X, 1.0, Dv, zmul(k, M, Cm), tmp, Q, 1.0, 0.0, Z, mM);
+          // QR: Q S = tmp
+          if (!zcholesky(k, gram(op, s, tmp, tmp), L)) {
+            breakdown = 1;
+            break;
+          }
+          const zmat S = zadj(k, L);
+          // Q = tmp S^-1 ; D = Q + D S^H
+          lincomb2(op, s, 3, Q, nullptr, 0.0, tmp, zinv_upper(k, S), Dn, nullptr, 0.0, 1.0, Dv, zadj(k, S));
+          std::swap(Dv, Dn);
+          Cm = zmul(k, S, Cm);
+          const zmat rr = zmul(k, zadj(k, Cm), Cm);
+          double worst = 0.0;
+          for (int b = 0; b < k; ++b) {
+            rel[b] = ssq[b] > 0.0 ? rr[(size_t)b * k + b].real() / ssq[b] : 0.0;
+            worst = std::max(worst, rel[b]);
+          }
+          iters = it + 1;
+          if (worst <= prm->eps * prm->eps) {
+            converged = 1;
+            break;
+          }
+        }
+      }
+    } else {
+      converged = 1;
+    }
+    // ---- reconstruct: x_D = A^-1 X ; x_C = A_C^-1 (src_C - Dhop G X) ----
+    op->local(s, D, X, xD, op->Ainv(false));
+    op->local(s, D, X, tC, op->G());
+    op->dslash(s, C, false, tC, s1, op->none(), -1.0, srcC, 1.0);
+    op->local(s, C, s1, xC, op->Ainv(false));
+    CK(cudaStreamSynchronize(s));
+    if (res) {
+      std::memset(res, 0, sizeof(*res));
+      res->iterations = iters;
+      res->converged = converged;
+      res->breakdown = breakdown;
+      for (int b = 0; b < k; ++b) res->residual_sq[b] = rel[b];
+    }
+  });
+}

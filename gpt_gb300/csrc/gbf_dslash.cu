@@ -275,16 +275,21 @@ static int sm_count() {
 }
 
 // Blocks of `kernel` resident per SM at block size bd and dynamic shared
-// memory smem (also raises the kernel's dynamic shared-memory limit when smem
-// exceeds the default 48 KB); cached per (kernel, bd, smem).
+// memory smem; cached per (kernel, bd, smem).  Also raises the kernel's
+// dynamic shared-memory limit to the largest smem requested so far (the limit
+// only grows, so every cached configuration stays launchable).
 int resident_blocks(const void* kernel, int bd, size_t smem) {
   static std::mutex mu;
   static std::map<std::tuple<const void*, int, size_t>, int> cache;
+  static std::map<const void*, size_t> limit;
   const auto key = std::make_tuple(kernel, bd, smem);
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 48 * 1024 && smem > limit[kernel]) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    limit[kernel] = smem;
+  }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, bd, smem) != cudaSuccess || nb < 1) {
     cudaGetLastError();

@@ -102,4 +102,16 @@ cudaError_t launch_clover_narrow_dd(const void* srcdd, void* dst32, long long nr
 // FP64 complex array -> double-float (float4 per complex), n_complex elements
 cudaError_t launch_split_dd(const void* src64, void* dst, long long n_complex, cudaStream_t st);
 
+// block CG (gbf_block.cu): Gram matrix out[i k + j] = sum conj(A_i) . B_j of the
+// k = nrhs packed vectors (partial: max_blocks x k x k entries; counter zero
+// on entry, restored), and out_i = beta Y_i + sum_j X_j W[j k + i]
+cudaError_t launch_gram(int P, const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
+                        unsigned* counter, double2* out, cudaStream_t st);
+cudaError_t launch_lincomb(int P, const Geo& g, void* out, const void* Y, double beta, const void* X, const double2* W,
+                           cudaStream_t st);
+// out1 = b1 Y1 + X1 W1 ; out2 = b2 Y2 + c out1 + X2 W2 in one pass
+cudaError_t launch_lincomb2(int P, const Geo& g, void* out1, const void* Y1, double b1, const void* X1, const double2* W1,
+                            void* out2, const void* Y2, double b2, double c, const void* X2, const double2* W2,
+                            cudaStream_t st);
+
 }  // namespace gbf

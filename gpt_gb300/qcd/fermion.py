@@ -197,6 +197,14 @@ class fermion_operator(matrix_operator):
 
         return _tune.tune(self, force=force)
 
+    # native eo2_ne + block CG on the device (gbf_solve_eo2ne_block_cg)
+    def _solve_eo2ne_block_cg(self, dst, src, eps, maxiter, graph_iterations=0, profile=0):
+        p = _lib.gbf_cg_params(float(eps), int(maxiter), 0, 0)
+        r = _lib.gbf_cg_result()
+        _lib.check(_lib.load().gbf_solve_eo2ne_block_cg(self.obj, src.ptr, dst.ptr, ctypes.byref(p), ctypes.byref(r),
+                                                        core.stream_ptr()))
+        return r
+
     # native eo2_ne + CG on the device (gbf_solve_eo2ne_cg)
     def _solve_eo2ne_cg(self, dst, src, eps, maxiter, graph_iterations=0, profile=0):
         p = _lib.gbf_cg_params(float(eps), int(maxiter), int(graph_iterations), int(profile))

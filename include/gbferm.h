@@ -147,6 +147,18 @@ typedef struct {
 } gbf_cg_result;
 int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* p, gbf_cg_result* res, void* stream);
 
+/* preconditioned(eo2_ne(), block_cg(eps, maxiter)) on device
+ * (lib/gpt/algorithms/inverter/block_cg.py:36-149): the n_rhs packed
+ * right-hand sides share one Krylov space (block CG with a Cholesky QR of the
+ * residual block).  Gram matrices are reduced on the device and the k x k
+ * algebra runs on the host, two reads per iteration; zero initial guess.
+ * Converged when max_b (C^H C)_bb / |b_b|^2 <= eps^2 (the reference's test).
+ * All right-hand sides must be non-zero and linearly independent (otherwise
+ * the QR breaks down: breakdown = 1).  iterations_per_graph and profile are
+ * ignored; residual_sq[b] is the block recursion's (C^H C)_bb / |b_b|^2. */
+int gbf_solve_eo2ne_block_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* p, gbf_cg_result* res,
+                             void* stream);
+
 /* Autotuner (the role of lib/gpt/core/auto_tune.py for this library): times
  * the block-size candidates of the four kernel classes -- [0] hopping kernel
  * with a per-thread epilogue, [1] hopping kernel with the Mobius s-matrix
