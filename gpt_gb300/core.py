@@ -8,6 +8,7 @@ host layout, complex128 [V, (Ls,) 4, 3].  All arithmetic runs on the GPU
 through libgbferm.so; PyTorch only provides device memory and streams.
 """
 import ctypes
+import threading
 
 import numpy as np
 import torch
@@ -83,30 +84,51 @@ def stream_ptr():
 _layout_cache = {}
 
 
+class _native_handle:
+    """A native operator handle (the vector-algebra workspace of a layout),
+    deleted with the object."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        try:
+            _lib.load().gbf_delete(self.h)
+        except Exception:
+            pass
+
+
 class layout:
-    """Field layout = (4D grid, Ls, n_rhs).  Owns a light-weight native
-    operator handle used for vector algebra on fields of this layout."""
+    """Field layout = (4D grid, Ls, n_rhs).  Owns light-weight native
+    operator handles used for vector algebra on fields of this layout, one
+    per thread: a handle carries reduction workspace, and the C ABI allows one
+    thread per handle at a time (worker threads of the serving loop reduce
+    fields of the same layout concurrently on their own streams)."""
+
+    _create_lock = threading.Lock()
 
     def __init__(self, g, Ls=1, n_rhs=1):
         self.grid = g
         self.Ls = int(Ls)
         self.n_rhs = int(n_rhs)
         self.five_d = self.Ls > 1 or False
-        self._op = None
+        self._local = threading.local()
 
     @staticmethod
     def get(g, Ls=1, n_rhs=1, five_d=None):
         key = (tuple(g.fdimensions), g.precision.name, int(Ls), int(n_rhs), bool(five_d))
-        lay = _layout_cache.get(key)
-        if lay is None:
-            lay = layout(g, Ls, n_rhs)
-            lay.five_d = bool(five_d) if five_d is not None else Ls > 1
-            _layout_cache[key] = lay
+        with layout._create_lock:
+            lay = _layout_cache.get(key)
+            if lay is None:
+                lay = layout(g, Ls, n_rhs)
+                lay.five_d = bool(five_d) if five_d is not None else Ls > 1
+                _layout_cache[key] = lay
         return lay
 
     @property
     def op(self):
-        if self._op is None:
+        hd = getattr(self._local, "handle", None)
+        if hd is None:
             L = _lib.load()
             p = _lib.gbf_params()
             for i in range(4):
@@ -119,8 +141,9 @@ class layout:
             h = ctypes.c_void_p()
             name = b"mobius" if self.five_d else b"wilson_clover"
             _lib.check(L.gbf_create(name, self.grid.precision.code, ctypes.byref(p), ctypes.byref(h)))
-            self._op = h
-        return self._op
+            hd = _native_handle(h)
+            self._local.handle = hd
+        return hd.h
 
     def half_bytes(self):
         N = self.grid.gsites // 2 * self.Ls * self.n_rhs
@@ -130,12 +153,6 @@ class layout:
         V = self.grid.gsites
         return (V, self.Ls, 4, 3) if self.five_d else (V, 4, 3)
 
-    def __del__(self):
-        try:
-            if self._op is not None:
-                _lib.load().gbf_delete(self._op)
-        except Exception:
-            pass
 
 
 class lattice:

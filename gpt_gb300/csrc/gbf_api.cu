@@ -335,7 +335,11 @@ void build_smat(gbf_op* op) {
 
 void ensure_ws(gbf_op* op) {
   if (op->partial) return;
-  const long long maxblocks = op->g.Vh + 1;
+  // reducing launches use at most one wave of resident blocks (<= 32 per SM)
+  // or, for the double-float hop, up to 4096 blocks (reduce_grid)
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long maxblocks = std::min<long long>(op->g.Vh + 1, (long long)sms * 32 + 4096);
   op->partial = (double2*)dmalloc((size_t)maxblocks * op->g.nrhs * sizeof(double2));
   op->counter = (unsigned*)dmalloc(sizeof(unsigned) * 4);
   CK(cudaMemset(op->counter, 0, sizeof(unsigned) * 4));

@@ -92,8 +92,11 @@ def test_gpu_request_same_alone_and_in_mix():
     if not torch.cuda.is_available():
         pytest.skip("needs a GPU")
     ex = serving.gpu_executor(keep_solution=True)
+    # requests 4 and 5 share lattice size and source count (so the field
+    # layout) with 0 and 1: concurrent reductions on the same layout
     reqs = [serving.Request(0, 8, 0.3, 11, 0.1, 2, 21), serving.Request(1, 16, 0.4, 12, 0.05, 3, 22),
-            serving.Request(2, 8, 0.25, 13, 0.2, 1, 23), serving.Request(3, 16, 0.3, 14, 0.1, 1, 24)]
+            serving.Request(2, 8, 0.25, 13, 0.2, 1, 23), serving.Request(3, 16, 0.3, 14, 0.1, 1, 24),
+            serving.Request(4, 8, 0.35, 15, 0.15, 2, 25), serving.Request(5, 16, 0.45, 16, 0.08, 3, 26)]
     alone = {}
     for r in reqs:
         res, _ = serving.Server(ex, 1 << 36, realtime=False).run([r])
