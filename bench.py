@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=40, help="c5: number of requests")
     ap.add_argument("--inner", default="single", choices=["single", "half"], help="c3/c4 inner precision")
     ap.add_argument("--rhs-group", type=int, default=0, help="c4: right-hand sides solved together (0: auto)")
+    ap.add_argument("--with-plain", action="store_true",
+                    help="c3: also time one plain FP64 and one plain double-float packed solve of the same sources")
     ap.add_argument("--solver", default="cg", choices=["cg", "block_cg"],
                     help="c3/c4 inner solver: independent CG per packed rhs, or block CG over them")
     return ap.parse_args()
@@ -211,6 +213,43 @@ def run_mobius_config(args, which):
         nr, nb = ([nr], [nb]) if group == 1 else (nr, nb)
         worst = max(worst, max(math.sqrt(a / b) for a, b in zip(nr, nb)))
     value = nsrc * args.steps / (total_ms / 1000.0)
+    plain = {}
+    if args.with_plain and ngroups == 1:
+        # the same packed sources with the plain method: eo2_ne CG in FP64
+        # and in double-float, to the same true residual
+        for name, pop in [("plain_fp64", op), ("plain_double_float", op.converted(g.double_float))]:
+            # eps on the eo2_ne normal residual; tol / 10 makes the true 5D
+            # residual of M x = b reach tol (measured ratio about 6)
+            pcg = inv.cg({"eps": tol / 10, "maxiter": 50000, "iterations_per_graph": 16})
+            psolve = inv.preconditioned(pc.eo2_ne(), pcg)(pop)
+            s4 = srcs[0]
+            if pop is not op:
+                s4c = pop.U_lattice()
+                g.convert(s4c, s4)
+                s4 = s4c
+            b5 = pop.ImportPhysicalFermionSource(s4)
+            torch.cuda.synchronize()
+            q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            q0.record(stream)
+            x5 = psolve(b5)
+            pop.ExportPhysicalFermionSolution(x5)
+            q1.record(stream)
+            torch.cuda.synchronize()
+            ms = q0.elapsed_time(q1)
+            xr = op.F_lattice()
+            g.convert(xr, x5)
+            b5r = op.F_lattice()
+            g.convert(b5r, b5)
+            r5 = op.F_lattice()
+            op.M(r5, xr)
+            g.axpby(r5, -1.0, r5, 1.0, b5r)
+            nr, nb = g.norm2(r5), g.norm2(b5r)
+            nr, nb = ([nr], [nb]) if group == 1 else (nr, nb)
+            plain[name] = {"solves_per_s": nsrc / (ms / 1000.0), "ms_per_step": ms, "cg_iterations": pcg.last.iterations,
+                           "true_residual_5d": max(math.sqrt(a / b) for a, b in zip(nr, nb))}
+            del psolve, x5, b5, xr, b5r, r5
+        plain["mixed_over_plain_fp64"] = value / plain["plain_fp64"]["solves_per_s"]
+        plain["mixed_over_plain_double_float"] = value / plain["plain_double_float"]["solves_per_s"]
     cfg = {"workload": f"mobius {'x'.join(map(str, dims))} Ls {Ls} b 1.5 c 0.5 M5 1.8 mass {mass} gauge eps {geps}, "
                        f"{nsrc} {'point' if which == 'c3' else 'gaussian'} sources in {ngroups} packed group(s) of {group}, "
                        f"propagator Export*solve*Import, defect correction ({args.inner} inner {args.solver}, tol {inner_tol}) "
@@ -219,7 +258,7 @@ def run_mobius_config(args, which):
     line = _common_line(METRIC, value, "solves/s", args, 1, total_ms, cfg, f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",
                         {"gpu_launches": int(n1 - n0), "clocks": clk, "true_residual_5d": worst,
                          "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
-                         "ms_per_solve": total_ms / args.steps / nsrc})
+                         "ms_per_solve": total_ms / args.steps / nsrc, **plain})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -509,7 +548,9 @@ def run_gbf(args, dims):
                                eps=CFG["tol"], maxiter=100)
     solver = dc(op)
     inner_op = dc.inner_inverter.inner_op  # the FP32 operator built by mixed_precision
-    plain_cg = inv.cg({"eps": CFG["tol"], "maxiter": 40000, "iterations_per_graph": 16})
+    # the plain CG's eps bounds the eo2_ne normal residual; tol / 3 brings the
+    # true residual of M x = b below tol (eps = tol leaves it at 1.5 tol)
+    plain_cg = inv.cg({"eps": CFG["tol"] / 3, "maxiter": 40000, "iterations_per_graph": 16})
     plain = inv.preconditioned(pc.eo2_ne(), plain_cg)(op)
 
     V = grid.gsites
@@ -634,7 +675,7 @@ def run_gbf(args, dims):
     op_dd = op.converted(g.double_float)
     src_dd = op_dd.F_lattice()
     src_dd[:] = src_np
-    dd_cg = inv.cg({"eps": CFG["tol"], "maxiter": 40000, "iterations_per_graph": 16})
+    dd_cg = inv.cg({"eps": CFG["tol"] / 3, "maxiter": 40000, "iterations_per_graph": 16})
     plain_dd = inv.preconditioned(pc.eo2_ne(), dd_cg)(op_dd)
     xq = plain_dd(src_dd)
     dd_it = dd_cg.last.iterations

@@ -213,7 +213,7 @@ def gpu_executor(keep_solution=False, inner_tol=1e-5):
     """executor for Server: Wilson-clover (csw 1.0, phases [1,1,1,-1]) on a
     fresh device-generated gauge field; mixed = defect_correcting(
     mixed_precision(preconditioned(eo2_ne, cg(inner_tol))), single, double);
-    plain = preconditioned(eo2_ne, cg(tol)) in FP64."""
+    plain = preconditioned(eo2_ne, cg(tol / 3)) in FP64."""
     import ctypes
 
     import torch
@@ -242,7 +242,9 @@ def gpu_executor(keep_solution=False, inner_tol=1e-5):
                     inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": inner_tol, "maxiter": 20000})),
                                         core.single, core.double), eps=req.tol, maxiter=100)(op)
             else:
-                solver = inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": req.tol, "maxiter": 40000}))(op)
+                # eps bounds the eo2_ne normal residual; tol / 3 brings the true
+                # residual of M x = b below tol (eps = tol leaves about 2 tol)
+                solver = inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": req.tol / 3, "maxiter": 40000}))(op)
             x = solver(src)
             r = op.F_lattice()
             op.M(r, x)
