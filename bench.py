@@ -139,10 +139,27 @@ def run_mobius_config(args, which):
         group = 12
     else:
         dims, Ls, mass, geps, tol, nsrc = [32, 32, 32, 64], 16, 0.005, 0.4, 1e-10, 12
-        group = args.rhs_group or 2
+        group = args.rhs_group
     grid = g.grid(dims, g.double)
     U = g.qcd.gauge.random_su3_device(grid, geps, 4242)
     inner_prec = g.half if args.inner == "half" else g.single
+    rhs_tuning = None
+    if not group:
+        # RHS block size by the autotuner: time 3 inner CG iterations of the
+        # packed inner operator per candidate that fits (the outer FP64 loop
+        # needs about as much memory again: budget half the free memory)
+        from gpt_gb300 import tune as _tune
+
+        base = dict(Ls=Ls, b=1.5, c=0.5, M5=1.8, mass_plus=mass, mass_minus=mass, boundary_phases=[1.0, 1.0, 1.0, -1.0])
+        free, _ = torch.cuda.mem_get_info()
+        # whole mixed solve per rhs: about 8 FP64 and 7 FP32 full 5D fields
+        per_rhs = 8 * 192 * grid.gsites * Ls + 7 * 96 * grid.gsites * Ls
+        cands = [k for k in (1, 2, 3, 4, 6) if k * per_rhs <= 0.85 * free]
+        rhs_tuning = _tune.rhs_group(
+            lambda k: g.qcd.fermion.mobius_operator(U, dict(base, n_rhs=k), precision=inner_prec), nsrc,
+            candidates=cands, budget_bytes=int(0.85 * free))
+        group = rhs_tuning["params"][0]
+        torch.cuda.empty_cache()
     inner_tol = 1e-5 if args.inner == "single" else 3e-3
     V = grid.gsites
     ngroups = (nsrc + group - 1) // group
@@ -258,7 +275,8 @@ def run_mobius_config(args, which):
     line = _common_line(METRIC, value, "solves/s", args, 1, total_ms, cfg, f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",
                         {"gpu_launches": int(n1 - n0), "clocks": clk, "true_residual_5d": worst,
                          "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
-                         "ms_per_solve": total_ms / args.steps / nsrc, **plain})
+                         "ms_per_solve": total_ms / args.steps / nsrc, **plain,
+                         **({"rhs_group_tuning": rhs_tuning["results"]} if rhs_tuning else {})})
     print(json.dumps(line), flush=True)
     return 0
 

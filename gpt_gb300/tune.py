@@ -49,7 +49,7 @@ def load(tag):
     try:
         with open(fn, "rt") as f:
             data = json.load(f)
-        if data.get("tag") != tag or len(data.get("params", [])) != 4:
+        if data.get("tag") != tag or not data.get("params"):
             return None
     except (OSError, ValueError):
         return None
@@ -81,7 +81,7 @@ def tune(op, force=False, stream=None):
     tag = tag_of(op)
     if not force:
         data = load(tag)
-        if data is not None:
+        if data is not None and len(data["params"]) == 4:
             apply(op, data["params"])
             return data
     bd = (ctypes.c_int * 4)()
@@ -89,3 +89,75 @@ def tune(op, force=False, stream=None):
     s = core.stream_ptr() if stream is None else stream
     _lib.check(_lib.load().gbf_tune(op.obj, s, bd, us))
     return save(tag, list(bd), list(us))
+
+
+def rhs_group(make_op, n_sources, candidates=None, budget_bytes=None, iterations=3, tag=None, force=False):
+    """Choose how many right-hand sides to pack into one operator (the RHS
+    block size) by timing `iterations` eo2_ne CG iterations of the packed
+    operator for each candidate size and minimising the time of all groups,
+    ceil(n_sources / k) * t_iteration(k).
+
+    make_op(k) builds the operator that the solve spends its time in (the
+    inner-precision one) with n_rhs = k.  Candidates whose device footprint,
+    extrapolated from the memory the k = 1 trial used, would not fit
+    `budget_bytes` (default: 80 % of the free device memory) are skipped.
+    Returns {"tag", "params": [k], "results": [[k, ms per iteration], ...]};
+    cached like the block sizes when `tag` is given."""
+    import math
+
+    import torch
+
+    from . import core
+
+    if tag is not None and not force:
+        data = load(tag)
+        if data is not None:
+            return data
+    if candidates is None:
+        candidates = [k for k in range(1, min(n_sources, 16) + 1) if n_sources % k == 0]
+    free0, _ = torch.cuda.mem_get_info()
+    budget = budget_bytes if budget_bytes is not None else int(0.8 * free0)
+    L = _lib.load()
+    results = []
+    per_rhs = None
+    for k in sorted(candidates):
+        if per_rhs is not None and k * per_rhs > budget:
+            continue
+        torch.cuda.synchronize()
+        before = torch.cuda.mem_get_info()[0]
+        op = make_op(k)
+        b = op.F_lattice()
+        x = op.F_lattice()
+        # a seeded Gaussian source for every packed right-hand side
+        V = b.layout.grid.gsites * b.layout.Ls
+        nat = torch.empty(V * 24, dtype=torch.float64, device="cuda")
+        for j in range(k):
+            _lib.check(L.gbf_random_spinor(V * 12, 7 + j, nat.data_ptr(), core.stream_ptr()))
+            _lib.check(L.gbf_field_import(b.layout.op, nat.data_ptr(), b.ptr, j, int(b.layout.five_d), core.stream_ptr()))
+        del nat
+        op._solve_eo2ne_cg(x, b, 1e-30, 1, 0, 1)  # warm-up (allocates the workspace)
+        torch.cuda.synchronize()
+        used = before - torch.cuda.mem_get_info()[0]
+        r = op._solve_eo2ne_cg(x, b, 1e-30, iterations, 0, 1)
+        ms = sum(r.kernel_ms) / max(1, r.iterations)
+        results.append([k, ms])
+        if per_rhs is None:
+            per_rhs = max(1, used)
+        del op, b, x
+        torch.cuda.synchronize()
+    best = min(results, key=lambda kr: math.ceil(n_sources / kr[0]) * kr[1])
+    data = {"tag": tag, "params": [int(best[0])], "results": [[int(k), float(ms)] for k, ms in results]}
+    if tag is not None:
+        data = save_rhs(tag, data)
+    return data
+
+
+def save_rhs(tag, data):
+    fn = cache_file(tag)
+    os.makedirs(os.path.dirname(fn) or ".", exist_ok=True)
+    tmp = fn + f".{os.getpid()}.tmp"
+    with open(tmp, "wt") as f:
+        json.dump(data, f)
+    os.replace(tmp, fn)
+    _runtime_cache[fn] = data
+    return data

@@ -119,3 +119,29 @@ def _to(op, arr):
     lat = op.F_lattice()
     lat[:] = arr
     return lat
+
+
+def test_rhs_group_cache_record(tmp_path, monkeypatch):
+    monkeypatch.setenv("GPT_GB300_TUNE_DIR", str(tmp_path))
+    T._runtime_cache.clear()
+    rec = T.save_rhs("rhs/mobius/test", {"tag": "rhs/mobius/test", "params": [3], "results": [[1, 2.0], [3, 5.0]]})
+    T._runtime_cache.clear()
+    assert T.load("rhs/mobius/test")["params"] == [3] and rec["results"][1] == [3, 5.0]
+
+
+@gpu
+def test_rhs_group_tuner_picks_a_timed_candidate(tmp_path, monkeypatch):
+    _need_gpu()
+    import gpt_gb300 as g
+
+    monkeypatch.setenv("GPT_GB300_TUNE_DIR", str(tmp_path))
+    T._runtime_cache.clear()
+    dims = [4, 4, 4, 8]
+    U = g.qcd.gauge.random_su3(g.grid(dims, g.double), 0.4, 3)
+    base = dict(Ls=4, b=1.5, c=0.5, M5=1.8, mass_plus=0.1, mass_minus=0.1, boundary_phases=[1, 1, 1, -1])
+    rec = T.rhs_group(lambda k: g.qcd.fermion.mobius_operator(U, dict(base, n_rhs=k), precision=g.single), 4,
+                      candidates=[1, 2, 4], tag="rhs/test")
+    assert [r[0] for r in rec["results"]] == [1, 2, 4]
+    assert all(r[1] > 0 for r in rec["results"])
+    assert rec["params"][0] in (1, 2, 4)
+    assert T.rhs_group(None, 4, tag="rhs/test")["params"] == rec["params"]  # cached
