@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-dslash", action="store_true",
                     help="profiling case: one operator only, one eo2_ne CG of 12 iterations")
-    ap.add_argument("--profile-precision", default="single", choices=["single", "double", "double_float"],
+    ap.add_argument("--profile-precision", default="single", choices=["single", "double", "double_float", "half"],
                     help="precision of the --profile-dslash operator")
     ap.add_argument("--profile-mobius", action="store_true",
                     help="profiling case: FP32 mobius 12^3x24 Ls 12 with 12 packed rhs, 12 CG iterations")
@@ -110,8 +110,13 @@ def run_profile_mobius(args):
         op._solve_eo2ne_cg(x, src, 1e-30, 12)
     r = op._solve_eo2ne_cg(x, src, 1e-30, 12, 0, 1)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": "mobius FP32 12^3x24 Ls 12, 12 rhs, eo2_ne CG 12 iterations", "iterations": r.iterations,
-                      "kernel_ms": list(r.kernel_ms), "kernel_launches": list(r.kernel_launches)}))
+    out = {"profile_case": "mobius FP32 12^3x24 Ls 12, 12 rhs, eo2_ne CG 12 iterations", "iterations": r.iterations,
+           "kernel_ms": list(r.kernel_ms), "kernel_launches": list(r.kernel_launches)}
+    if args.solver == "block_cg":
+        rb = op._solve_eo2ne_block_cg(x, src, 1e-30, 4)
+        torch.cuda.synchronize()
+        out["block_cg_iterations"] = rb.iterations
+    print(json.dumps(out))
     return 0
 
 
@@ -390,7 +395,7 @@ def run_profile_case(args, dims):
     grid = g.grid(dims, g.double)
     U = g.qcd.gauge.random_su3(grid, CFG["gauge_eps"], CFG["gauge_seed"])
     params = dict(mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"], boundary_phases=CFG["phases"])
-    prec = {"single": g.single, "double": g.double, "double_float": g.double_float}[args.profile_precision]
+    prec = {"single": g.single, "double": g.double, "double_float": g.double_float, "half": g.half}[args.profile_precision]
     op = g.qcd.fermion.wilson_clover_operator(U, params, precision=prec)
     V = grid.gsites
     rng = np.random.default_rng(CFG["src_seed"])
