@@ -38,6 +38,7 @@ class gbf_params(ctypes.Structure):
         ("c", ctypes.c_double),
         ("M5", ctypes.c_double),
         ("reconstruct", ctypes.c_int),
+        ("mu", ctypes.c_double),
     ]
 
 

@@ -83,6 +83,8 @@ struct gbf_op {
   double cc[4];
   double diag = 0;  // 1/(2 kappa) for wilson_clover
   bool has_clover = false;
+  bool twisted = false;  // wilson_twisted_mass: Mooee = diag + i mu g5
+  double mu = 0;
   bool gauge_set = false;
   void* links = nullptr;
   void* clov_mem = nullptr;      // clover + inverse, both parities, op precision
@@ -140,10 +142,25 @@ struct gbf_op {
     }
     return l;
   }
-  LocalOp G() const { return mobius ? smat_slot(S_G) : clover(true); }
-  LocalOp Gdag() const { return mobius ? smat_slot(S_GDAG) : clover(true); }
-  LocalOp A(bool dag) const { return mobius ? smat_slot(dag ? S_ADAG : S_A) : clover(false); }
-  LocalOp Ainv(bool dag) const { return mobius ? smat_slot(dag ? S_AINVDAG : S_AINV) : clover(true); }
+  // twisted mass: (a + i mu g5), inverse (a - i mu g5) / (a^2 + mu^2), adjoints conjugate
+  LocalOp twist(bool inv, bool dag) const {
+    LocalOp l{};
+    l.kind = LOC_TWIST;
+    const double a = diag, den = inv ? a * a + mu * mu : 1.0;
+    double b = (inv ? -mu : mu) / den;
+    if (dag) b = -b;
+    l.z[0] = a / den;
+    l.z[1] = b;   // spins 0, 1 (g5 = +1)
+    l.z[2] = a / den;
+    l.z[3] = -b;  // spins 2, 3 (g5 = -1)
+    return l;
+  }
+  LocalOp G() const { return mobius ? smat_slot(S_G) : twisted ? twist(true, false) : clover(true); }
+  LocalOp Gdag() const { return mobius ? smat_slot(S_GDAG) : twisted ? twist(true, true) : clover(true); }
+  LocalOp A(bool dag) const { return mobius ? smat_slot(dag ? S_ADAG : S_A) : twisted ? twist(false, dag) : clover(false); }
+  LocalOp Ainv(bool dag) const {
+    return mobius ? smat_slot(dag ? S_AINVDAG : S_AINV) : twisted ? twist(true, dag) : clover(true);
+  }
   LocalOp B(bool dag) const { return smat_slot(dag ? S_BDAG : S_B); }
 
   RedArgs red(int fin) const { RedArgs r; r.fin = fin; r.partial = partial; r.counter = counter; r.st = st; return r; }
@@ -408,7 +425,8 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
     if (!name || !params || !out) throw Fail(GBF_E_ARG, "null argument");
     *out = nullptr;
     std::string nm(name);
-    if (nm != "wilson_clover" && nm != "mobius") throw Fail(GBF_E_UNSUPPORTED, "unknown fermion operator " + nm);
+    if (nm != "wilson_clover" && nm != "mobius" && nm != "wilson_twisted_mass")
+      throw Fail(GBF_E_UNSUPPORTED, "unknown fermion operator " + nm);
     if (precision < GBF_DOUBLE || precision > GBF_DOUBLE_FLOAT) throw Fail(GBF_E_ARG, "bad precision");
     const gbf_params& p = *params;
     for (int m = 0; m < 4; ++m)
@@ -436,6 +454,14 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
       op->cc[3] = 1.0;
       op->diag = p.mass + 1.0 + 3.0 * nu / xi0;
       op->has_clover = (p.csw_r != 0.0 || p.csw_t != 0.0);
+      if (nm == "wilson_twisted_mass") {
+        if (op->has_clover || xi0 != 1.0 || nu != 1.0) {
+          delete op;
+          throw Fail(GBF_E_UNSUPPORTED, "wilson_twisted_mass is isotropic and has no clover term");
+        }
+        op->twisted = true;
+        op->mu = p.mu;
+      }
     }
     setup_geo(op);
     try {

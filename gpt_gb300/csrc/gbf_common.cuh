@@ -30,7 +30,7 @@ namespace gbf {
 // see struct dd below), the FP64-accurate path that runs on the FP32 pipe.
 enum Prec { P64 = 0, P32 = 1, P16 = 2, PDD = 3 };
 enum LinkStore { L64 = 0, L32 = 1, L32R = 2, LDD = 3 };
-enum LocalKind { LOC_NONE = 0, LOC_CLOVER = 1, LOC_SMAT = 2, LOC_SCALAR = 3 };
+enum LocalKind { LOC_NONE = 0, LOC_CLOVER = 1, LOC_SMAT = 2, LOC_SCALAR = 3, LOC_TWIST = 4 };
 
 constexpr int kMaxLs = 32;
 constexpr int kMaxRhs = 16;

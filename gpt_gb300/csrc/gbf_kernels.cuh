@@ -14,11 +14,15 @@ namespace gbf {
 //   LOC_SMAT:   one real Ls x Ls matrix per chirality acting on the s index,
 //               the same at every 4D site; [2][Ls][Ls] in the arithmetic type.
 //   LOC_SCALAR: multiplication by a real constant.
+//   LOC_TWIST:  multiplication by a complex constant per chirality, z[0] + i z[1]
+//               on spins 0, 1 and z[2] + i z[3] on spins 2, 3 (twisted mass
+//               a + i mu g5, its inverse and adjoints).
 struct LocalOp {
   int kind;
   const void* clov[2];  // per parity
   const void* smat;
   double scalar;
+  double z[4];
 };
 
 template <typename R> struct CloverLoad;
@@ -145,6 +149,13 @@ template <typename R>
 __device__ __forceinline__ void local_apply_thread(const LocalOp& l, int Vh, int parity, int cb, cplx<R> (&v)[12]) {
   if (l.kind == LOC_CLOVER) {
     clover_apply<R>(l.clov[parity], Vh, cb, v);
+  } else if (l.kind == LOC_TWIST) {
+    const cplx<R> z0 = mk<R>((R)l.z[0], (R)l.z[1]), z1 = mk<R>((R)l.z[2], (R)l.z[3]);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      nrm<R>(v[k]);
+      v[k] = cmul<R>(k < 6 ? z0 : z1, v[k]);
+    }
   } else if (l.kind == LOC_SCALAR) {
     const R s = (R)l.scalar;
 #pragma unroll

@@ -1,4 +1,4 @@
-"""Fermion operators: g.qcd.fermion.wilson_clover and g.qcd.fermion.mobius.
+"""Fermion operators: g.qcd.fermion.wilson_clover, wilson_twisted_mass and mobius.
 
 Mirrors lib/gpt/qcd/fermion/wilson.py:63-96 (parameter handling, kappa ->
 mass), lib/gpt/qcd/fermion/mobius.py:25-117 and the operator object of
@@ -59,7 +59,11 @@ def _params_struct(name, p, dims, Ls, n_rhs):
         s.boundary_phases[2 * mu] = complex(ph[mu]).real
         s.boundary_phases[2 * mu + 1] = complex(ph[mu]).imag
     s.reconstruct = int(p.get("reconstruct", -1))
-    if name == "wilson_clover":
+    if name == "wilson_twisted_mass":
+        s.mass = float(p["mass"])
+        s.mu = float(p["mu"])
+        s.xi_0 = s.nu = 1.0
+    elif name == "wilson_clover":
         s.mass = float(p["mass"])
         s.csw_r = float(p.get("csw_r", 0.0))
         s.csw_t = float(p.get("csw_t", 0.0))
@@ -257,6 +261,23 @@ def wilson_clover(U, params=None, **kw):
 class wilson_clover_operator(fermion_operator):
     def __init__(self, U, params, precision=None, daggered=False, clover_from=None):
         super().__init__("wilson_clover", U, params, precision, daggered, clover_from)
+
+
+def wilson_twisted_mass(U, params=None, **kw):
+    """g.qcd.fermion.wilson_twisted_mass (lib/gpt/qcd/fermion/wilson.py:99-107):
+    the Wilson hop with Mooee = (4 + mass) + i mu gamma5 (Grid's WilsonTMFermion
+    through lib/cgpt/lib/operators/wilson_twisted_mass.h:19-45)."""
+    p = _std_params(params, kw)
+    for k in ("mass", "mu", "boundary_phases"):
+        if p.get(k) is None:
+            raise ValueError(f"{k} required")
+    p.setdefault("n_rhs", 1)
+    return wilson_twisted_mass_operator(U, p)
+
+
+class wilson_twisted_mass_operator(fermion_operator):
+    def __init__(self, U, params, precision=None, daggered=False, clover_from=None):
+        super().__init__("wilson_twisted_mass", U, params, precision, daggered)
 
 
 def mobius(U, params=None, **kw):

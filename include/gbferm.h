@@ -68,10 +68,12 @@ typedef struct {
   double boundary_phases[8];  /* 4 complex numbers (re, im) */
   double mass_plus, mass_minus, b, c, M5;
   int reconstruct;            /* -1 auto, 0: 18 reals per link, 1: 12 reals (SU(3), FP32/FP16) */
+  double mu;                  /* wilson_twisted_mass: Mooee = (4 + mass) + i mu gamma5 */
 } gbf_params;
 
-/* cgpt create_fermion_operator (operators.cc:34-57): name is "wilson_clover"
- * or "mobius".  Allocates device storage; the gauge field is set by
+/* cgpt create_fermion_operator (operators.cc:34-57): name is "wilson_clover",
+ * "wilson_twisted_mass" (operators/wilson_twisted_mass.h:19-45: isotropic
+ * Wilson hop, no clover) or "mobius".  Allocates device storage; the gauge field is set by
  * gbf_update_gauge before first use. */
 int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op** out);
 

@@ -71,6 +71,8 @@ def lib():
         L.orc_plaquette.argtypes = [P, P]
         L.orc_wilson_clover_new.restype = P
         L.orc_wilson_clover_new.argtypes = [P, P, D, D, D, D, D, P, I]
+        L.orc_wilson_twisted_mass_new.restype = P
+        L.orc_wilson_twisted_mass_new.argtypes = [P, P, D, D, P, I]
         L.orc_mobius_new.restype = P
         L.orc_mobius_new.argtypes = [P, P, I, D, D, D, D, D, P, I]
         L.orc_op_free.argtypes = [P]
@@ -293,6 +295,22 @@ class wilson_clover(_op):
         ph = _phases(boundary_phases)
         self.obj = lib().orc_wilson_clover_new(_ptr(self.U), _ptr(d), float(mass), float(csw_r), float(csw_t),
                                                float(xi_0), float(nu), _ptr(ph), int(with_single))
+        if not self.obj:
+            raise RuntimeError(lib().orc_last_error().decode())
+
+
+class wilson_twisted_mass(_op):
+    """g.qcd.fermion.wilson_twisted_mass parameters (lib/gpt/qcd/fermion/wilson.py:99-107):
+    Wilson hop, Mooee = (4 + mass) + i mu g5."""
+
+    def __init__(self, U, dims, mass, mu, boundary_phases=(1, 1, 1, -1), with_single=False, **_ignored):
+        self.dims = list(dims)
+        self.V = int(np.prod(dims))
+        self.U = np.ascontiguousarray(U, dtype=np.complex128)
+        d = np.array(dims, dtype=np.int64)
+        ph = _phases(boundary_phases)
+        self.obj = lib().orc_wilson_twisted_mass_new(_ptr(self.U), _ptr(d), float(mass), float(mu), _ptr(ph),
+                                                     int(with_single))
         if not self.obj:
             raise RuntimeError(lib().orc_last_error().decode())
 

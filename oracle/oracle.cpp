@@ -779,6 +779,11 @@ struct WilsonClover : OpBase<T> {
   Hop<T> hop;
   bool has_clover = false;
   T diag = 0;                     // 1/(2 kappa)
+  // twisted mass: Mooee = diag + i mu g5, g5 = diag(1, 1, -1, -1) in the gpt
+  // basis (lib/cgpt/lib/operators/wilson_twisted_mass.h:19-45 -> Grid's
+  // WilsonTMFermion, statement of the fingerprint in
+  // tests/qcd/fermion_operators.py:366-386)
+  double mu = 0.0;
   std::vector<cx<T>> clov, clov_inv;  // [site][2][36]
   using OpBase<T>::G;
   void build(const Geom* g, const double* Uin, double m0, double csw_r, double csw_t, double xi_0, double nu,
@@ -857,6 +862,18 @@ struct WilsonClover : OpBase<T> {
       const long x = list ? (*list)[i] : i;
       const cx<T>* p = in + (size_t)x * 12;
       cx<T>* o = out + (size_t)x * 12;
+      if (!has_clover && mu != 0.0) {
+        // (a + i mu g5), its inverse (a - i mu g5) / (a^2 + mu^2), adjoints conjugate
+        const double a = (double)diag, den = inv ? a * a + mu * mu : 1.0;
+        for (int k = 0; k < 12; ++k) {
+          const double g5 = k < 6 ? 1.0 : -1.0;
+          double zi = (inv ? -mu : mu) * g5 / den;
+          if (dag) zi = -zi;
+          const cx<T> z = {(T)(a / den), (T)zi};
+          o[k] = cmul(z, p[k]);
+        }
+        continue;
+      }
       if (!has_clover) {
         const T f = inv ? (T)(1.0 / (double)diag) : diag;  // 2 kappa for the inverse
         for (int k = 0; k < 12; ++k) o[k] = cscale(f, p[k]);
@@ -1185,6 +1202,29 @@ void* orc_wilson_clover_new(const double* U, const long* dims, double m0, double
     if (with_single) {
       auto ws = std::make_unique<WilsonClover<float>>();
       ws->build(o->G.get(), U, m0, csw_r, csw_t, xi_0, nu, phases);
+      o->f = std::move(ws);
+    }
+    return o;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+
+// twisted-mass Wilson operator (isotropic, no clover)
+void* orc_wilson_twisted_mass_new(const double* U, const long* dims, double m0, double mu, const double* phases,
+                                  int with_single) {
+  try {
+    auto o = new OracleOp;
+    o->G = std::make_unique<Geom>(dims);
+    auto w = std::make_unique<WilsonClover<double>>();
+    w->build(o->G.get(), U, m0, 0.0, 0.0, 1.0, 1.0, phases);
+    w->mu = mu;
+    o->d = std::move(w);
+    if (with_single) {
+      auto ws = std::make_unique<WilsonClover<float>>();
+      ws->build(o->G.get(), U, m0, 0.0, 0.0, 1.0, 1.0, phases);
+      ws->mu = mu;
       o->f = std::move(ws);
     }
     return o;

@@ -9,7 +9,9 @@ are extracted -- no code -- from:
   tests/random/simple.py:17-31           plaquettes of g.qcd.gauge.random
   tests/random/simple.py:66-127          normal() samples at five coordinates
   tests/random/simple.py:129-141         rng.choice() results
-  tests/qcd/fermion_operators.py:338-524 Grid operator fingerprints
+  tests/qcd/fermion_operators.py:338-524 Grid operator fingerprints (wilson,
+                                         wilson_clover, wilson_twisted_mass,
+                                         mobius, mobius_axial_mass, zmobius)
 """
 import ast
 import json
@@ -32,6 +34,27 @@ def lit(src, name):
         if isinstance(node, ast.Assign) and any(isinstance(t, ast.Name) and t.id == name for t in node.targets):
             return node.value
     raise KeyError(name)
+
+
+def num(node):
+    """Literal numbers and the complex expressions a + 1j * (b) of the test file."""
+    if isinstance(node, ast.Constant):
+        return node.value
+    if isinstance(node, ast.UnaryOp) and isinstance(node.op, ast.USub):
+        return -num(node.operand)
+    if isinstance(node, ast.UnaryOp) and isinstance(node.op, ast.UAdd):
+        return num(node.operand)
+    if isinstance(node, ast.BinOp):
+        a, b = num(node.left), num(node.right)
+        if isinstance(node.op, ast.Add):
+            return a + b
+        if isinstance(node.op, ast.Sub):
+            return a - b
+        if isinstance(node.op, ast.Mult):
+            return a * b
+    if isinstance(node, ast.List):
+        return [num(e) for e in node.elts]
+    raise ValueError(ast.dump(node))
 
 
 def cplx_list(node):
@@ -73,21 +96,23 @@ out["sha256"] = {"cite": "tests/core/checksums.py:11-21", "input": re.search(r't
 
 fo = read("tests/qcd/fermion_operators.py")
 params = {}
-for pname in ["wilson_params", "wilson_clover_params"]:
+for pname in ["wilson_params", "wilson_clover_params", "wilson_twisted_mass_params"]:
     node = lit(fo, pname)
     params[pname] = {ast.literal_eval(k): ast.literal_eval(v) for k, v in zip(node.keys, node.values)}
 mats = {}
-for mname in ["wilson_matrices", "wilson_clover_matrices"]:
+for mname in ["wilson_matrices", "wilson_clover_matrices", "wilson_twisted_mass_matrices"]:
     node = lit(fo, mname)
     mats[mname] = {ast.literal_eval(k): cplx_list(v)[0] for k, v in zip(node.keys, node.values)}
 suite = lit(fo, "test_suite")
 mob = {}
 for k, v in zip(suite.keys, suite.values):
     key = ast.literal_eval(k)
-    if key not in ("mobius", "mobius_axial_mass"):
+    if key not in ("mobius", "mobius_axial_mass", "zmobius"):
         continue
     d = {ast.literal_eval(kk): vv for kk, vv in zip(v.keys, v.values)}
-    p = {ast.literal_eval(kk): ast.literal_eval(vv) for kk, vv in zip(d["params"].keys, d["params"].values)}
+    p = {ast.literal_eval(kk): num(vv) for kk, vv in zip(d["params"].keys, d["params"].values)}
+    if "omega" in p:  # complex numbers as [re, im] pairs
+        p["omega"] = [[complex(w).real, complex(w).imag] for w in p["omega"]]
     mm = {ast.literal_eval(kk): cplx_list(vv)[0] for kk, vv in zip(d["matrices"].keys, d["matrices"].values)}
     mob[key] = {"params": p, "matrices": mm}
 out["fingerprints"] = {
@@ -97,6 +122,7 @@ out["fingerprints"] = {
     "rel_tol": 1e-13,
     "wilson": {"params": params["wilson_params"], "matrices": mats["wilson_matrices"]},
     "wilson_clover": {"params": params["wilson_clover_params"], "matrices": mats["wilson_clover_matrices"]},
+    "wilson_twisted_mass": {"params": params["wilson_twisted_mass_params"], "matrices": mats["wilson_twisted_mass_matrices"]},
     **mob,
 }
 with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json"), "w") as f:

@@ -38,6 +38,8 @@ def gpu_op(kind, U, dims, prec, **p):
     Uf = g.qcd.gauge.gauge_field(grid, U)
     if kind == "wilson_clover":
         op = g.qcd.fermion.wilson_clover(Uf, p)
+    elif kind == "wilson_twisted_mass":
+        op = g.qcd.fermion.wilson_twisted_mass(Uf, p)
     else:
         op = g.qcd.fermion.mobius(Uf, p)
     return op if prec is g.double else op.converted(prec)
@@ -86,6 +88,20 @@ def test_gpu_wilson_clover_fingerprints(name, prec):
 
 
 @pytest.mark.parametrize("prec", ["double", "double_float"])
+def test_gpu_twisted_mass_fingerprint(prec):
+    fp = GOLD["fingerprints"]
+    dims = fp["grid"]
+    case = fp["wilson_twisted_mass"]
+    f = _fp_fields(dims)
+    op = gpu_op("wilson_twisted_mass", f["U"], dims, PREC[prec], **case["params"])
+    src = to_gpu(op, f["src4"])
+    for tag, ref in case["matrices"].items():
+        dst = op.M(src) if tag == "" else op.Mdiag(src)
+        X = np.vdot(f["dst4"].ravel(), dst[:].ravel())
+        assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (tag, X)
+
+
+@pytest.mark.parametrize("prec", ["double", "double_float"])
 @pytest.mark.parametrize("name", ["mobius", "mobius_axial_mass"])
 def test_gpu_mobius_fingerprints(name, prec):
     fp = GOLD["fingerprints"]
@@ -112,11 +128,14 @@ def test_gpu_mobius_fingerprints(name, prec):
 WC = dict(mass=0.1, csw_r=1.0, csw_t=1.0, boundary_phases=[1.0, 1.0, 1.0, -1.0])
 WC_ANISO = dict(mass=-0.2, csw_r=1.2, csw_t=0.7, xi_0=1.3, nu=2.1, boundary_phases=[1.0, -1.0, 1j, np.exp(0.3j)])
 MOB = dict(Ls=6, b=1.5, c=0.5, M5=1.8, mass_plus=0.05, mass_minus=0.09, boundary_phases=[1.0, 1.0, 1.0, -1.0])
+TM = dict(mass=0.1, mu=0.3, boundary_phases=[1.0, 1.0, 1.0, -1.0])
 
 
 def _oracle(kind, U, dims, p):
     if kind == "wilson_clover":
         return o.wilson_clover(U, dims, **p)
+    if kind == "wilson_twisted_mass":
+        return o.wilson_twisted_mass(U, dims, **p)
     return o.mobius(U, dims, **{k: v for k, v in p.items() if k != "n_rhs"})
 
 
@@ -126,6 +145,7 @@ def _oracle(kind, U, dims, p):
     ("wilson_clover", WC_ANISO, [4, 2, 6, 4]),
     ("wilson_clover", dict(mass=0.3, boundary_phases=[1, 1, 1, -1]), [2, 2, 2, 2]),
     ("mobius", MOB, [4, 4, 2, 4]),
+    ("wilson_twisted_mass", TM, [4, 4, 4, 8]),
 ])
 def test_opcodes_vs_oracle(kind, params, dims, prec):
     P = PREC[prec]
@@ -197,7 +217,8 @@ def test_multi_rhs_packed_equals_single():
 # solvers
 # ---------------------------------------------------------------------------
 @pytest.mark.parametrize("prec", ["double", "double_float"])
-@pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1))])
+@pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1)),
+                                         ("wilson_twisted_mass", TM)])
 def test_eo2ne_cg_vs_oracle(kind, params, prec):
     dims = [4, 4, 4, 8]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 21).U

@@ -94,6 +94,19 @@ def test_wilson_clover_fingerprints(name):
         assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (name, tag, X)
 
 
+def test_wilson_twisted_mass_fingerprint():
+    """tests/qcd/fermion_operators.py:366-386, 519-523: Grid's WilsonTMFermion."""
+    fp = GOLD["fingerprints"]
+    dims = fp["grid"]
+    case = fp["wilson_twisted_mass"]
+    f = _fingerprint_fields(dims)
+    op = o.wilson_twisted_mass(f["U"], dims, **case["params"])
+    for tag, ref in case["matrices"].items():
+        opname = {"": "M", ".Mdiag": "Mdiag"}[tag]
+        X = o.inner(f["dst4"], op.apply(opname, f["src4"]))
+        assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (tag, X)
+
+
 @pytest.mark.parametrize("name", ["mobius", "mobius_axial_mass"])
 def test_mobius_fingerprints(name):
     fp = GOLD["fingerprints"]
