@@ -73,6 +73,8 @@ def lib():
         L.orc_wilson_clover_new.argtypes = [P, P, D, D, D, D, D, P, I]
         L.orc_wilson_twisted_mass_new.restype = P
         L.orc_wilson_twisted_mass_new.argtypes = [P, P, D, D, P, I]
+        L.orc_zmobius_new.restype = P
+        L.orc_zmobius_new.argtypes = [P, P, I, P, P, D, D, D, P, I, I]
         L.orc_mobius_new.restype = P
         L.orc_mobius_new.argtypes = [P, P, I, D, D, D, D, D, P, I]
         L.orc_op_free.argtypes = [P]
@@ -350,6 +352,34 @@ class mobius(_op):
         _check(lib().orc_op_apply(self.obj, OPCODES["ExportPhysicalFermionSolution"], _ptr(x5), _ptr(out), FULL))
         return out
 
+
+
+class zmobius(mobius):
+    """g.qcd.fermion.zmobius parameters (lib/gpt/qcd/fermion/zmobius.py:59-78):
+    Ls = len(omega), per-slice complex b_s = ((b + c) / omega_s + (b - c)) / 2,
+    c_s = ((b + c) / omega_s - (b - c)) / 2.  col_scale selects which slice
+    index scales the c_s K term (output slice by default)."""
+
+    def __init__(self, U, dims, omega, b, c, M5, mass=None, mass_plus=None, mass_minus=None,
+                 boundary_phases=(1, 1, 1, -1), with_single=False, col_scale=False, **_ignored):
+        if mass is not None:
+            mass_plus = mass_minus = mass
+        om = [complex(*w) if isinstance(w, (list, tuple)) else complex(w) for w in omega]
+        Ls = len(om)
+        bs = np.array([0.5 * ((b + c) / w + (b - c)) for w in om], dtype=np.complex128)
+        cs = np.array([0.5 * ((b + c) / w - (b - c)) for w in om], dtype=np.complex128)
+        self.bs, self.cs = bs, cs
+        self.dims = list(dims)
+        self.V = int(np.prod(dims))
+        self.n5 = Ls
+        self.U = np.ascontiguousarray(U, dtype=np.complex128)
+        d = np.array(dims, dtype=np.int64)
+        ph = _phases(boundary_phases)
+        self.obj = lib().orc_zmobius_new(_ptr(self.U), _ptr(d), int(Ls), _ptr(bs), _ptr(cs), float(M5),
+                                         float(mass_plus), float(mass_minus), _ptr(ph), int(with_single),
+                                         int(bool(col_scale)))
+        if not self.obj:
+            raise RuntimeError(lib().orc_last_error().decode())
 
 def inner(a, b):
     return complex(np.vdot(a.ravel(), b.ravel()))

@@ -908,56 +908,78 @@ struct Mobius : OpBase<T> {
   Hop<T> hop;
   int Ls;
   double b, c, M5, mp, mm;
-  std::vector<cd> Ainv[2], A[2];  // [chirality][Ls*Ls], chirality 0 = P+ (spins 0,1)
+  // per-slice Cayley coefficients (zmobius: complex, from omega; mobius: b, c)
+  // and the dense per-chirality matrices B = diag(bs) + diag(cs) K (cs scales
+  // the output slice; col_scale: K diag(cs), the input slice)
+  std::vector<cd> bs, cs;
+  bool col_scale = false;
+  std::vector<cd> Ainv[2], A[2], B[2];  // [chirality][Ls*Ls], chirality 0 = P+ (spins 0,1)
   using OpBase<T>::G;
   using OpBase<T>::n5;
   void build(const Geom* g, const double* Uin, int Ls_, double b_, double c_, double M5_, double mp_, double mm_,
              const double* phases) {
+    std::vector<cd> vb(Ls_, cd{b_, 0}), vc(Ls_, cd{c_, 0});
+    build_z(g, Uin, Ls_, vb, vc, M5_, mp_, mm_, phases, false);
+    b = b_;
+    c = c_;
+  }
+  void build_z(const Geom* g, const double* Uin, int Ls_, const std::vector<cd>& bs_, const std::vector<cd>& cs_,
+               double M5_, double mp_, double mm_, const double* phases, bool col) {
     G = g;
-    Ls = Ls_; n5 = Ls; b = b_; c = c_; M5 = M5_; mp = mp_; mm = mm_;
+    Ls = Ls_; n5 = Ls; M5 = M5_; mp = mp_; mm = mm_;
+    bs = bs_; cs = cs_; col_scale = col;
+    b = bs[0].re; c = cs[0].re;
     hop.load(G, Uin, phases, 1.0);
-    double dg = (4.0 - M5) * b + 1.0, od = (4.0 - M5) * c - 1.0;
     for (int ch = 0; ch < 2; ++ch) {
-      A[ch].assign(Ls * Ls, cd{0, 0});
-      for (int s = 0; s < Ls; ++s) A[ch][s * Ls + s] = {dg, 0};
+      std::vector<double> K(Ls * Ls, 0.0);
       for (int s = 0; s < Ls; ++s) {
         if (ch == 0) {  // P+: couples s to s-1, wall term at s=0 from Ls-1
-          if (s >= 1) A[ch][s * Ls + s - 1] = cadd(A[ch][s * Ls + s - 1], cd{od, 0});
-          else A[ch][0 * Ls + Ls - 1] = cadd(A[ch][Ls - 1], cd{-mp * od, 0});
+          if (s >= 1) K[s * Ls + s - 1] = 1.0;
+          else K[Ls - 1] = -mp;
         } else {  // P-: couples s to s+1, wall term at s=Ls-1 from 0
-          if (s <= Ls - 2) A[ch][s * Ls + s + 1] = cadd(A[ch][s * Ls + s + 1], cd{od, 0});
-          else A[ch][(Ls - 1) * Ls + 0] = cadd(A[ch][(Ls - 1) * Ls], cd{-mm * od, 0});
+          if (s <= Ls - 2) K[s * Ls + s + 1] = 1.0;
+          else K[(Ls - 1) * Ls] = -mm;
         }
       }
+      B[ch].assign(Ls * Ls, cd{0, 0});
+      A[ch].assign(Ls * Ls, cd{0, 0});
+      for (int s = 0; s < Ls; ++s)
+        for (int t = 0; t < Ls; ++t) {
+          const double k = K[s * Ls + t];
+          cd v = (s == t) ? bs[s] : cd{0, 0};
+          if (k != 0.0) v = cadd(v, cscale(k, col_scale ? cs[t] : cs[s]));
+          B[ch][s * Ls + t] = v;
+          cd a = cscale(4.0 - M5, v);
+          if (s == t) a.re += 1.0;
+          a.re -= k;
+          A[ch][s * Ls + t] = a;
+        }
       Ainv[ch].resize(Ls * Ls);
       if (!invert_cmat(Ls, A[ch].data(), Ainv[ch].data())) throw std::runtime_error("singular Mooee");
     }
   }
-  // (b + cK) psi or its adjoint, per 4D site of the given parity
+  // B psi or B^+ psi, per 4D site of the given parity
   void mix(cx<T>* out, const cx<T>* in, int parity, bool dag) const {
     const std::vector<int32_t>* list = parity < 2 ? &G->par_sites[parity] : nullptr;
     const long n = list ? (long)list->size() : G->V;
-    const T tb = (T)b, tc = (T)c, tmp_ = (T)mp, tmm = (T)mm;
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < n; ++i) {
       const long x = list ? (*list)[i] : i;
       const cx<T>* p = in + (size_t)x * Ls * 12;
       cx<T>* o = out + (size_t)x * Ls * 12;
-      for (int s = 0; s < Ls; ++s) {
-        cx<T> r[12];
-        for (int k = 0; k < 12; ++k) r[k] = cscale(tb, p[s * 12 + k]);
-        // upper spins (P+): K couples s <- s-1 (adjoint: s <- s+1)
-        int sp;
-        T f;
-        if (!dag) { sp = s - 1; f = tc; if (s == 0) { sp = Ls - 1; f = -tmp_ * tc; } }
-        else { sp = s + 1; f = tc; if (s == Ls - 1) { sp = 0; f = -tmp_ * tc; } }
-        for (int k = 0; k < 6; ++k) r[k] = cadd(r[k], cscale(f, p[sp * 12 + k]));
-        // lower spins (P-): K couples s <- s+1 (adjoint: s <- s-1)
-        if (!dag) { sp = s + 1; f = tc; if (s == Ls - 1) { sp = 0; f = -tmm * tc; } }
-        else { sp = s - 1; f = tc; if (s == 0) { sp = Ls - 1; f = -tmm * tc; } }
-        for (int k = 6; k < 12; ++k) r[k] = cadd(r[k], cscale(f, p[sp * 12 + k]));
-        for (int k = 0; k < 12; ++k) o[s * 12 + k] = r[k];
-      }
+      std::vector<cx<T>> r((size_t)Ls * 12);
+      for (int ch = 0; ch < 2; ++ch)
+        for (int s = 0; s < Ls; ++s)
+          for (int k = 6 * ch; k < 6 * ch + 6; ++k) {
+            cx<T> acc = {0, 0};
+            for (int t = 0; t < Ls; ++t) {
+              const cd m = dag ? cd{B[ch][t * Ls + s].re, -B[ch][t * Ls + s].im} : B[ch][s * Ls + t];
+              if (m.re == 0.0 && m.im == 0.0) continue;
+              acc = cadd(acc, cmul(cx<T>{(T)m.re, (T)m.im}, p[t * 12 + k]));
+            }
+            r[s * 12 + k] = acc;
+          }
+      for (size_t k = 0; k < r.size(); ++k) o[k] = r[k];
     }
   }
   void Dhop(cx<T>* out, const cx<T>* in, int out_parity, bool dag) const override { hop.apply(out, in, out_parity, dag, Ls); }
@@ -1268,15 +1290,17 @@ int orc_op_apply(void* o, int opcode, const double* in, double* out, int parity)
       int Ls = m.Ls;
       size_t len = (size_t)G.V * Ls * 12;
       if (opcode == OP_DMINUS || opcode == OP_DMINUS_DAG) {
-        // Dminus psi_s = psi_s - c D_W psi_s, D_W = (4 - M5) + Dhop (slice-wise)
+        // Dminus psi_s = psi_s - c_s D_W psi_s, D_W = (4 - M5) + Dhop (slice-wise);
+        // the adjoint takes conj(c_s)
         std::vector<cd> t(len);
         m.hop.apply(t.data(), i, 2, opcode == OP_DMINUS_DAG, Ls);
-        double cc = m.c;
-        if (opcode == OP_DMINUS_DAG) cc = m.c;  // real c: adjoint has the same coefficient
 #pragma omp parallel for
         for (long k = 0; k < (long)len; ++k) {
+          const int sl = (int)((k / 12) % Ls);
+          cd cc = m.cs[sl];
+          if (opcode == OP_DMINUS_DAG) cc.im = -cc.im;
           cd dw = cadd(t[k], cscale(4.0 - m.M5, i[k]));
-          out_[k] = csub(i[k], cscale(cc, dw));
+          out_[k] = csub(i[k], cmul(cc, dw));
         }
         return;
       }
@@ -1291,6 +1315,34 @@ int orc_op_apply(void* o, int opcode, const double* in, double* out, int parity)
     }
     apply_full(op.d.get(), opcode, out_, i, parity);
   });
+}
+
+// zmobius: per-slice complex b_s, c_s (2 Ls doubles each, re/im pairs);
+// col_scale selects K diag(c) instead of diag(c) K
+void* orc_zmobius_new(const double* U, const long* dims, int Ls, const double* bs, const double* cs, double M5,
+                      double mass_plus, double mass_minus, const double* phases, int with_single, int col_scale) {
+  try {
+    auto o = new OracleOp;
+    o->mobius = true;
+    o->G = std::make_unique<Geom>(dims);
+    std::vector<cd> vb(Ls), vc(Ls);
+    for (int s = 0; s < Ls; ++s) {
+      vb[s] = {bs[2 * s], bs[2 * s + 1]};
+      vc[s] = {cs[2 * s], cs[2 * s + 1]};
+    }
+    auto m = std::make_unique<Mobius<double>>();
+    m->build_z(o->G.get(), U, Ls, vb, vc, M5, mass_plus, mass_minus, phases, col_scale != 0);
+    o->d = std::move(m);
+    if (with_single) {
+      auto ms = std::make_unique<Mobius<float>>();
+      ms->build_z(o->G.get(), U, Ls, vb, vc, M5, mass_plus, mass_minus, phases, col_scale != 0);
+      o->f = std::move(ms);
+    }
+    return o;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
 }
 
 // Mobius source import: the 4D source is placed on the walls with the chiral

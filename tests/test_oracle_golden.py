@@ -107,6 +107,24 @@ def test_wilson_twisted_mass_fingerprint():
         assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (tag, X)
 
 
+def test_zmobius_fingerprint():
+    """tests/qcd/fermion_operators.py:400-426: Grid's ZMobiusFermion, complex
+    per-slice b_s, c_s from omega (lib/gpt/qcd/fermion/zmobius.py:31-34), the
+    c_s K term scaled by the output slice."""
+    fp = GOLD["fingerprints"]
+    dims = fp["grid"]
+    case = fp["zmobius"]
+    p = case["params"]
+    f = _fingerprint_fields(dims, Ls=len(p["omega"]))
+    op = o.zmobius(f["U"], dims, **p)
+    for tag, ref in case["matrices"].items():
+        if tag == ".ImportPhysicalFermionSource":
+            X = o.inner(f["dst5"], op.import_physical_source(f["src4"]))
+        else:
+            X = o.inner(f["dst5"], op.apply("M" if tag == "" else "Mdiag", f["src5"]))
+        assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (tag, X)
+
+
 @pytest.mark.parametrize("name", ["mobius", "mobius_axial_mass"])
 def test_mobius_fingerprints(name):
     fp = GOLD["fingerprints"]
