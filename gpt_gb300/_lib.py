@@ -39,6 +39,7 @@ class gbf_params(ctypes.Structure):
         ("M5", ctypes.c_double),
         ("reconstruct", ctypes.c_int),
         ("mu", ctypes.c_double),
+        ("omega", ctypes.c_void_p),
     ]
 
 

@@ -68,7 +68,9 @@ void* dmalloc(size_t bytes) {
 }
 
 // Mobius s-matrix slots (real Ls x Ls per chirality)
-enum { S_A = 0, S_ADAG, S_AINV, S_AINVDAG, S_B, S_BDAG, S_G, S_GDAG, S_COUNT };
+// (DM1, DMC: the diagonal parts of Dminus = DM1 + DMC Dhop, per-slice
+//  1 - c_s (4 - M5) and -c_s, used when c_s varies with s)
+enum { S_A = 0, S_ADAG, S_AINV, S_AINVDAG, S_B, S_BDAG, S_G, S_GDAG, S_DM1, S_DM1DAG, S_DMC, S_DMCDAG, S_COUNT };
 
 }  // namespace
 
@@ -90,8 +92,10 @@ struct gbf_op {
   void* clov_mem = nullptr;      // clover + inverse, both parities, op precision
   void* clov[2] = {nullptr, nullptr};
   void* clov_inv[2] = {nullptr, nullptr};
-  void* smat = nullptr;          // [S_COUNT][2][Ls][Ls] in the arithmetic precision
-  std::vector<double> smat_host; // same in double
+  void* smat = nullptr;          // [S_COUNT][2][Ls][Ls] in the arithmetic precision ((re, im) pairs if complex)
+  bool smat_cplx = false;        // zmobius: complex per-slice coefficients
+  bool zmobius = false;
+  std::vector<std::complex<double>> bs, cs;  // Cayley coefficients per slice
   // workspace
   void* pair_mem[6] = {};        // workspace: full fields allocated on first use
   void* tmp[12] = {};
@@ -127,7 +131,8 @@ struct gbf_op {
   LocalOp smat_slot(int s) const {
     LocalOp l{};
     l.kind = LOC_SMAT;
-    l.smat = (const char*)smat + (size_t)s * 2 * g.Ls * g.Ls * rb();
+    l.cplx = smat_cplx ? 1 : 0;
+    l.smat = (const char*)smat + (size_t)s * 2 * g.Ls * g.Ls * (smat_cplx ? 2 : 1) * rb();
     return l;
   }
   LocalOp clover(bool inv) const {
@@ -269,38 +274,24 @@ void setup_geo(gbf_op* op) {
   op->g4.fLs = FastDiv(1u);
 }
 
-// Cayley s-matrices of the Mobius operator with constant b_s = b, c_s = c
-// (lib/gpt/qcd/fermion/mobius.py:29-46).  With K+ the s-1 -> s hop with the
-// wall term -m+ at (0, Ls-1) and K- the s+1 -> s hop with -m- at (Ls-1, 0):
-//   A = (4-M5)(b + cK) + 1 - K  (Mooee),  B = b + cK,  G = B A^-1.
-void invert_real(int n, std::vector<double> a, std::vector<double>& inv) {
-  inv.assign(n * n, 0.0);
-  for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0;
-  for (int c = 0; c < n; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < n; ++r)
-      if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
-    if (a[piv * n + c] == 0.0) throw Fail(GBF_E_ARG, "singular Mooee (check M5, b, c, masses)");
-    for (int k = 0; k < n; ++k) { std::swap(a[c * n + k], a[piv * n + k]); std::swap(inv[c * n + k], inv[piv * n + k]); }
-    double d = 1.0 / a[c * n + c];
-    for (int k = 0; k < n; ++k) { a[c * n + k] *= d; inv[c * n + k] *= d; }
-    for (int r = 0; r < n; ++r) {
-      if (r == c) continue;
-      double f = a[r * n + c];
-      if (f == 0.0) continue;
-      for (int k = 0; k < n; ++k) { a[r * n + k] -= f * a[c * n + k]; inv[r * n + k] -= f * inv[c * n + k]; }
-    }
-  }
-}
-
+// Cayley s-matrices of the Mobius / zmobius operator with per-slice b_s, c_s
+// (mobius: b, c for every s, lib/gpt/qcd/fermion/mobius.py:29-46; zmobius:
+// b_s = ((b + c) / omega_s + (b - c)) / 2, c_s = ((b + c) / omega_s - (b - c)) / 2,
+// lib/gpt/qcd/fermion/zmobius.py:31-34).  With K+ the s-1 -> s hop with the
+// wall term -m+ at (0, Ls-1) and K- the s+1 -> s hop with -m- at (Ls-1, 0),
+// c_s scaling the output slice (the convention that reproduces the
+// reference's zmobius fingerprint):
+//   B = diag(b) + diag(c) K,  A = (4 - M5) B + 1 - K  (Mooee),  G = B A^-1.
+// Adjoint slots hold conjugate transposes.
 void build_smat(gbf_op* op) {
+  using zc = std::complex<double>;
   const int Ls = op->g.Ls;
   const gbf_params& p = op->par;
-  const double dg = (4.0 - p.M5) * p.b + 1.0, od = (4.0 - p.M5) * p.c - 1.0;
-  std::vector<double> all((size_t)S_COUNT * 2 * Ls * Ls, 0.0);
-  auto slot = [&](int s, int ch) { return all.data() + ((size_t)s * 2 + ch) * Ls * Ls; };
+  const int L2 = Ls * Ls;
+  std::vector<zc> all((size_t)S_COUNT * 2 * L2, zc(0.0, 0.0));
+  auto slot = [&](int sl, int ch) { return all.data() + ((size_t)sl * 2 + ch) * L2; };
   for (int ch = 0; ch < 2; ++ch) {
-    std::vector<double> K(Ls * Ls, 0.0), A(Ls * Ls), B(Ls * Ls), Ai, G(Ls * Ls, 0.0);
+    std::vector<double> K(L2, 0.0);
     for (int s = 0; s < Ls; ++s) {
       if (ch == 0) {
         if (s >= 1) K[s * Ls + s - 1] = 1.0;
@@ -310,42 +301,88 @@ void build_smat(gbf_op* op) {
         else K[(Ls - 1) * Ls] = -p.mass_minus;
       }
     }
-    for (int i = 0; i < Ls * Ls; ++i) {
-      const double I = (i % (Ls + 1) == 0) ? 1.0 : 0.0;
-      A[i] = dg * I + od * K[i];
-      B[i] = p.b * I + p.c * K[i];
+    std::vector<zc> A(L2), B(L2), Ai(L2, zc(0.0, 0.0)), G(L2, zc(0.0, 0.0));
+    for (int s = 0; s < Ls; ++s)
+      for (int t = 0; t < Ls; ++t) {
+        const double k = K[s * Ls + t];
+        const zc bv = (s == t ? op->bs[s] : zc(0.0, 0.0)) + k * op->cs[s];
+        B[s * Ls + t] = bv;
+        A[s * Ls + t] = (4.0 - p.M5) * bv + (s == t ? 1.0 : 0.0) - k;
+      }
+    // Gauss-Jordan inverse of A with partial pivoting
+    std::vector<zc> a = A;
+    for (int i = 0; i < Ls; ++i) Ai[i * Ls + i] = 1.0;
+    for (int c = 0; c < Ls; ++c) {
+      int piv = c;
+      for (int r = c + 1; r < Ls; ++r)
+        if (std::abs(a[r * Ls + c]) > std::abs(a[piv * Ls + c])) piv = r;
+      if (std::abs(a[piv * Ls + c]) == 0.0) throw Fail(GBF_E_ARG, "singular Mooee (check M5, b, c, omega, masses)");
+      for (int k = 0; k < Ls; ++k) {
+        std::swap(a[c * Ls + k], a[piv * Ls + k]);
+        std::swap(Ai[c * Ls + k], Ai[piv * Ls + k]);
+      }
+      const zc d = 1.0 / a[c * Ls + c];
+      for (int k = 0; k < Ls; ++k) {
+        a[c * Ls + k] *= d;
+        Ai[c * Ls + k] *= d;
+      }
+      for (int r = 0; r < Ls; ++r) {
+        if (r == c) continue;
+        const zc f = a[r * Ls + c];
+        if (f == zc(0.0, 0.0)) continue;
+        for (int k = 0; k < Ls; ++k) {
+          a[r * Ls + k] -= f * a[c * Ls + k];
+          Ai[r * Ls + k] -= f * Ai[c * Ls + k];
+        }
+      }
     }
-    invert_real(Ls, A, Ai);
     for (int i = 0; i < Ls; ++i)
       for (int j = 0; j < Ls; ++j) {
-        double s = 0;
-        for (int k = 0; k < Ls; ++k) s += B[i * Ls + k] * Ai[k * Ls + j];
-        G[i * Ls + j] = s;
+        zc acc(0.0, 0.0);
+        for (int k = 0; k < Ls; ++k) acc += B[i * Ls + k] * Ai[k * Ls + j];
+        G[i * Ls + j] = acc;
       }
-    auto put = [&](int sl, const std::vector<double>& M, bool tr) {
-      double* d = slot(sl, ch);
+    std::vector<zc> DM1(L2, zc(0.0, 0.0)), DMC(L2, zc(0.0, 0.0));
+    for (int s = 0; s < Ls; ++s) {
+      DM1[s * Ls + s] = 1.0 - op->cs[s] * (4.0 - p.M5);
+      DMC[s * Ls + s] = -op->cs[s];
+    }
+    auto put = [&](int sl, const std::vector<zc>& M, bool adj) {
+      zc* d = slot(sl, ch);
       for (int i = 0; i < Ls; ++i)
-        for (int j = 0; j < Ls; ++j) d[i * Ls + j] = tr ? M[j * Ls + i] : M[i * Ls + j];
+        for (int j = 0; j < Ls; ++j) d[i * Ls + j] = adj ? std::conj(M[j * Ls + i]) : M[i * Ls + j];
     };
     put(S_A, A, false); put(S_ADAG, A, true);
     put(S_AINV, Ai, false); put(S_AINVDAG, Ai, true);
     put(S_B, B, false); put(S_BDAG, B, true);
     put(S_G, G, false); put(S_GDAG, G, true);
+    put(S_DM1, DM1, false); put(S_DM1DAG, DM1, true);
+    put(S_DMC, DMC, false); put(S_DMCDAG, DMC, true);
   }
-  op->smat_host = all;
-  if (!op->smat) op->smat = dmalloc(all.size() * op->rb());
+  // real storage unless a coefficient is complex
+  op->smat_cplx = false;
+  for (const zc& v : all)
+    if (v.imag() != 0.0) op->smat_cplx = true;
+  std::vector<double> flat;
+  flat.reserve(all.size() * 2);
+  for (const zc& v : all) {
+    flat.push_back(v.real());
+    if (op->smat_cplx) flat.push_back(v.imag());
+  }
+  const size_t bytes = all.size() * 2 * op->rb();  // room for the complex layout
+  if (!op->smat) op->smat = dmalloc(bytes);
   if (op->prec == P64) {
-    CK(cudaMemcpy(op->smat, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(op->smat, flat.data(), flat.size() * 8, cudaMemcpyHostToDevice));
   } else if (op->prec == PDD) {
-    std::vector<float> f(2 * all.size());
-    for (size_t i = 0; i < all.size(); ++i) {
-      const dd v(all[i]);
+    std::vector<float> f(2 * flat.size());
+    for (size_t i = 0; i < flat.size(); ++i) {
+      const dd v(flat[i]);
       f[2 * i] = v.h;
       f[2 * i + 1] = v.l;
     }
     CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
   } else {
-    std::vector<float> f(all.begin(), all.end());
+    std::vector<float> f(flat.begin(), flat.end());
     CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
   }
 }
@@ -425,15 +462,17 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
     if (!name || !params || !out) throw Fail(GBF_E_ARG, "null argument");
     *out = nullptr;
     std::string nm(name);
-    if (nm != "wilson_clover" && nm != "mobius" && nm != "wilson_twisted_mass")
+    if (nm != "wilson_clover" && nm != "mobius" && nm != "wilson_twisted_mass" && nm != "zmobius")
       throw Fail(GBF_E_UNSUPPORTED, "unknown fermion operator " + nm);
     if (precision < GBF_DOUBLE || precision > GBF_DOUBLE_FLOAT) throw Fail(GBF_E_ARG, "bad precision");
     const gbf_params& p = *params;
     for (int m = 0; m < 4; ++m)
       if (p.dims[m] < 2 || p.dims[m] % 2) throw Fail(GBF_E_ARG, "lattice dimensions must be even and >= 2");
     if (p.n_rhs < 1 || p.n_rhs > kMaxRhs) throw Fail(GBF_E_ARG, "n_rhs must be in [1, 16]");
-    const bool mob = nm == "mobius";
+    const bool zmob = nm == "zmobius";
+    const bool mob = nm == "mobius" || zmob;
     if (mob && (p.Ls < 1 || p.Ls > kMaxLs)) throw Fail(GBF_E_ARG, "Ls must be in [1, 32]");
+    if (zmob && !p.omega) throw Fail(GBF_E_ARG, "zmobius needs omega (2 Ls doubles)");
     const int N5 = (mob ? p.Ls : 1) * p.n_rhs;
     if (N5 > 256) throw Fail(GBF_E_ARG, "Ls * n_rhs must be <= 256");
     long long V = (long long)p.dims[0] * p.dims[1] * p.dims[2] * p.dims[3];
@@ -447,6 +486,22 @@ int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op
     if (mob) {
       for (int m = 0; m < 4; ++m) op->cc[m] = 1.0;
       op->diag = 4.0 - p.M5;
+      op->zmobius = zmob;
+      op->bs.assign(p.Ls, std::complex<double>(p.b, 0.0));
+      op->cs.assign(p.Ls, std::complex<double>(p.c, 0.0));
+      if (zmob) {
+        // lib/gpt/qcd/fermion/zmobius.py:31-34
+        for (int s = 0; s < p.Ls; ++s) {
+          const std::complex<double> w(p.omega[2 * s], p.omega[2 * s + 1]);
+          if (std::abs(w) == 0.0) {
+            delete op;
+            throw Fail(GBF_E_ARG, "omega must be non-zero");
+          }
+          op->bs[s] = 0.5 * ((p.b + p.c) / w + (p.b - p.c));
+          op->cs[s] = 0.5 * ((p.b + p.c) / w - (p.b - p.c));
+        }
+      }
+      op->par.omega = nullptr;  // not kept: the caller owns the array
     } else {
       const double xi0 = p.xi_0 != 0.0 ? p.xi_0 : 1.0;
       const double nu = p.nu != 0.0 ? p.nu : 1.0;
@@ -775,6 +830,16 @@ static void apply_one(gbf_op* op, int opcode, const void* src, void* dst, int sp
     case GBF_DMINUS_DAG: {
       if (!mob) {  // Wilson: Dminus is the identity (reference/wilson_clover.py:174-176)
         CK(cudaMemcpyAsync(dst, src, 2 * h, cudaMemcpyDeviceToDevice, s));
+        break;
+      }
+      if (op->zmobius) {
+        // per-slice c_s: Dminus = diag(1 - c_s (4 - M5)) + diag(-c_s) Dhop
+        // (diag(c_s) and Dhop commute; the adjoint conjugates c_s)
+        const bool dag = opcode == GBF_DMINUS_DAG;
+        for (int p = 0; p < 2; ++p) {
+          op->local(s, p, H(src, p), op->T(8), op->smat_slot(dag ? S_DM1DAG : S_DM1));
+          op->dslash(s, p, dag, H(src, 1 - p), HW(dst, p), op->smat_slot(dag ? S_DMCDAG : S_DMC), 1.0, op->T(8), 1.0);
+        }
         break;
       }
       // psi - c D_W psi, D_W = (4 - M5) + Dhop, slice by slice

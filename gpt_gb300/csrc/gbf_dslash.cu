@@ -38,7 +38,7 @@ namespace gbf {
 // shared memory: after the s-matrix tile and the reduction scratch.
 __host__ __device__ inline unsigned dd_acc_offset16(int LK, unsigned bd) {
   size_t s = 0;
-  if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * 8 + 8;
+  if (LK == LOC_SMAT) s += (24 * (size_t)bd + kSmatWords) * 8 + 8;
   s += 2 * (size_t)bd * 8;
   return (unsigned)((s + 15) / 16);
 }
@@ -206,7 +206,8 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
     if (a.l1.kind == LOC_SMAT) {
       R* tile = reinterpret_cast<R*>(smem_d);
       R* mat = tile + 24 * blockDim.x;
-      smat_apply_block<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res, true);
+      if (a.l1.cplx) smat_apply_block_c<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res);
+      else smat_apply_block<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res, true);
     }
   } else if (active && a.l1.kind != LOC_NONE) {
     if constexpr (P == PDD) {
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
   tile += gridDim.x;
   } while (LOOP && tile < ntiles);
   if (a.red) {
-    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
+    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + kSmatWords) * sizeof(R) / sizeof(double) + 1 : 0);
     block_reduce_finalize(a.ra, red_re, red_im, g.N5, g.Ls, g.nrhs, sm);
   }
 }
@@ -330,7 +331,7 @@ int pick_bd(int requested, int N5) {
 size_t dslash_smem_bytes(int P, int LK, int bd) {
   size_t rb = (P == P64 || P == PDD) ? 8 : 4;
   size_t s = 0;
-  if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
+  if (LK == LOC_SMAT) s += (24 * (size_t)bd + kSmatWords) * rb + 8;
   s += 2 * (size_t)bd * 8;
   if (P == PDD) s = 16 * (size_t)dd_acc_offset16(LK, bd) + 12 * 16 * (size_t)bd;  // + accumulators
   return s;

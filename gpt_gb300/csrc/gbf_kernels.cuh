@@ -21,6 +21,7 @@ struct LocalOp {
   int kind;
   const void* clov[2];  // per parity
   const void* smat;
+  int cplx;             // LOC_SMAT: complex matrices ([2][Ls][Ls] (re, im) pairs; zmobius)
   double scalar;
   double z[4];
 };
@@ -166,6 +167,10 @@ __device__ __forceinline__ void local_apply_thread(const LocalOp& l, int Vh, int
   }
 }
 
+// Shared-memory words reserved for the s-matrices of one block: two
+// chiralities of Ls x Ls complex entries at the largest Ls.
+constexpr int kSmatWords = 4 * kMaxLs * kMaxLs;
+
 // s-matrix op through shared memory.  Threads of one block hold complete
 // s-columns (blockDim is a multiple of N5, i5 = rhs*Ls + s fastest).
 // tile: 24*blockDim reals, one contiguous spinor per thread so the s-column
@@ -208,6 +213,51 @@ __device__ __forceinline__ void smat_apply_block(const R* mat_g, int Ls, R* tile
       for (int j = 0; j < per; ++j) {
         const int k = q * per + j;
         acc[k] = fma(k < 12 ? a0 : a1, e[j], acc[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 12; ++k) v[k] = mk<R>(acc[2 * k], acc[2 * k + 1]);
+  __syncthreads();
+}
+
+// The same with complex matrices ([2][Ls][Ls] entries of (re, im)), the
+// per-slice complex Cayley coefficients of zmobius.
+template <typename R>
+__device__ __forceinline__ void smat_apply_block_c(const R* mat_g, int Ls, R* tile, R* mat, cplx<R> (&v)[12]) {
+  using W = typename Vec4<R>::T;
+  constexpr int per = (int)(sizeof(W) / sizeof(R));  // reals per vector load (even)
+  const int t = threadIdx.x, bd = blockDim.x;
+  for (int k = t; k < 4 * Ls * Ls; k += bd) mat[k] = mat_g[k];
+  R* mine = tile + 24 * t;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    mine[2 * k] = v[k].x;
+    mine[2 * k + 1] = v[k].y;
+  }
+  __syncthreads();
+  const int s = t % Ls;
+  const R* col = tile + 24 * (t - s);
+  const R* m0 = mat + 2 * (s * Ls);
+  const R* m1 = mat + 2 * (Ls * Ls + s * Ls);
+  R acc[24];
+#pragma unroll
+  for (int k = 0; k < 24; ++k) acc[k] = rzero<R>();
+  for (int sp = 0; sp < Ls; ++sp) {
+    const R a0r = m0[2 * sp], a0i = m0[2 * sp + 1], a1r = m1[2 * sp], a1i = m1[2 * sp + 1];
+    const W* src = reinterpret_cast<const W*>(col + 24 * sp);
+#pragma unroll
+    for (int q = 0; q < 24 / per; ++q) {
+      const W w = src[q];
+      const R* e = reinterpret_cast<const R*>(&w);
+#pragma unroll
+      for (int j = 0; j < per; j += 2) {
+        const int k = q * per + j;
+        const R ar = k < 12 ? a0r : a1r, ai = k < 12 ? a0i : a1i;
+        acc[k] = fma(ar, e[j], acc[k]);
+        acc[k] = fma(-ai, e[j + 1], acc[k]);
+        acc[k + 1] = fma(ar, e[j + 1], acc[k + 1]);
+        acc[k + 1] = fma(ai, e[j], acc[k + 1]);
       }
     }
   }

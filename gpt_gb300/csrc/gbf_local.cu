@@ -49,7 +49,8 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
     if (a.l.kind == LOC_SMAT) {
       R* tile = reinterpret_cast<R*>(smem_d);
       R* mat = tile + 24 * blockDim.x;
-      smat_apply_block<R>(reinterpret_cast<const R*>(a.l.smat), g.Ls, tile, mat, v, true);
+      if (a.l.cplx) smat_apply_block_c<R>(reinterpret_cast<const R*>(a.l.smat), g.Ls, tile, mat, v);
+      else smat_apply_block<R>(reinterpret_cast<const R*>(a.l.smat), g.Ls, tile, mat, v, true);
     }
   } else if (active && a.l.kind != LOC_NONE) {
     local_apply_thread<R>(a.l, g.Vh, a.parity, cb, v);
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
   tile += gridDim.x;
   } while (LOOP && tile < ntiles);
   if (a.red) {
-    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + 2 * kMaxLs * kMaxLs) * sizeof(R) / sizeof(double) + 1 : 0);
+    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + kSmatWords) * sizeof(R) / sizeof(double) + 1 : 0);
     block_reduce_finalize(a.ra, red_re, red_im, g.N5, g.Ls, g.nrhs, sm);
   }
 }
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(256) local_kernel(const LocalArgs a) {
 static size_t local_smem(int P, int LK, int bd) {
   size_t rb = (P == P64 || P == PDD) ? 8 : 4;
   size_t s = 0;
-  if (LK == LOC_SMAT) s += (24 * (size_t)bd + 2 * kMaxLs * kMaxLs) * rb + 8;
+  if (LK == LOC_SMAT) s += (24 * (size_t)bd + kSmatWords) * rb + 8;
   return s + 2 * (size_t)bd * 8;
 }
 

@@ -77,6 +77,10 @@ def _params_struct(name, p, dims, Ls, n_rhs):
         s.c = float(p["c"])
         s.M5 = float(p["M5"])
         s.xi_0 = s.nu = 1.0
+        if name == "zmobius":
+            om = np.array([complex(w) for w in p["omega"]], dtype=np.complex128)
+            s.keep_omega = om  # alive until gbf_create has read it
+            s.omega = om.ctypes.data
     return s
 
 
@@ -91,10 +95,10 @@ class fermion_operator(matrix_operator):
         prec = precision if precision is not None else U.grid.precision
         self.U_grid = U.grid.converted(prec)
         self.precision = prec
-        self.Ls = int(params.get("Ls", 1)) if name == "mobius" else 1
+        self.Ls = int(params.get("Ls", 1)) if name in ("mobius", "zmobius") else 1
         self.n_rhs = int(params.get("n_rhs", 1))
         dims = self.U_grid.fdimensions
-        self.F_layout = core.layout.get(self.U_grid, self.Ls, self.n_rhs, five_d=name == "mobius")
+        self.F_layout = core.layout.get(self.U_grid, self.Ls, self.n_rhs, five_d=name in ("mobius", "zmobius"))
         self.U_layout = core.layout.get(self.U_grid, 1, self.n_rhs, five_d=False)
         L = _lib.load()
         s = _params_struct(name, self.params, dims, self.Ls, self.n_rhs)
@@ -290,6 +294,26 @@ def mobius(U, params=None, **kw):
         raise NotImplementedError("zmobius (omega) is not implemented on this path")
     p.setdefault("n_rhs", 1)
     return mobius_operator(U, p)
+
+
+def zmobius(U, params=None, **kw):
+    """g.qcd.fermion.zmobius (lib/gpt/qcd/fermion/zmobius.py:59-78): Ls =
+    len(omega), complex per-slice b_s, c_s from omega, b and c."""
+    p = _std_params(params, kw)
+    if p.get("omega") is None:
+        raise ValueError("omega required")
+    p["omega"] = [complex(*w) if isinstance(w, (list, tuple)) else complex(w) for w in p["omega"]]
+    p["Ls"] = len(p["omega"])
+    if p.get("mass") is not None:
+        p["mass_plus"] = p["mass"]
+        p["mass_minus"] = p["mass"]
+    p.setdefault("n_rhs", 1)
+    return zmobius_operator(U, p)
+
+
+class zmobius_operator(fermion_operator):
+    def __init__(self, U, params, precision=None, daggered=False, clover_from=None):
+        super().__init__("zmobius", U, params, precision, daggered)
 
 
 class mobius_operator(fermion_operator):

@@ -69,11 +69,13 @@ typedef struct {
   double mass_plus, mass_minus, b, c, M5;
   int reconstruct;            /* -1 auto, 0: 18 reals per link, 1: 12 reals (SU(3), FP32/FP16) */
   double mu;                  /* wilson_twisted_mass: Mooee = (4 + mass) + i mu gamma5 */
+  const double* omega;        /* zmobius: Ls complex omega_s as (re, im) pairs (read by gbf_create only) */
 } gbf_params;
 
 /* cgpt create_fermion_operator (operators.cc:34-57): name is "wilson_clover",
  * "wilson_twisted_mass" (operators/wilson_twisted_mass.h:19-45: isotropic
- * Wilson hop, no clover) or "mobius".  Allocates device storage; the gauge field is set by
+ * Wilson hop, no clover), "mobius" or "zmobius" (operators/zmobius.h: complex
+ * per-slice b_s, c_s from omega, lib/gpt/qcd/fermion/zmobius.py:31-34).  Allocates device storage; the gauge field is set by
  * gbf_update_gauge before first use. */
 int gbf_create(const char* name, int precision, const gbf_params* params, gbf_op** out);
 

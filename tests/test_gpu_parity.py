@@ -40,6 +40,8 @@ def gpu_op(kind, U, dims, prec, **p):
         op = g.qcd.fermion.wilson_clover(Uf, p)
     elif kind == "wilson_twisted_mass":
         op = g.qcd.fermion.wilson_twisted_mass(Uf, p)
+    elif kind == "zmobius":
+        op = g.qcd.fermion.zmobius(Uf, p)
     else:
         op = g.qcd.fermion.mobius(Uf, p)
     return op if prec is g.double else op.converted(prec)
@@ -88,6 +90,27 @@ def test_gpu_wilson_clover_fingerprints(name, prec):
 
 
 @pytest.mark.parametrize("prec", ["double", "double_float"])
+def test_gpu_zmobius_fingerprint(prec):
+    fp = GOLD["fingerprints"]
+    dims = fp["grid"]
+    case = fp["zmobius"]
+    p = case["params"]
+    f = _fp_fields(dims, len(p["omega"]))
+    op = gpu_op("zmobius", f["U"], dims, PREC[prec], **p)
+    src5 = to_gpu(op, f["src5"])
+    src4 = to_gpu(op, f["src4"], five=False)
+    for tag, ref in case["matrices"].items():
+        if tag == ".ImportPhysicalFermionSource":
+            out = op.ImportPhysicalFermionSource(src4)
+        elif tag == "":
+            out = op.M(src5)
+        else:
+            out = op.Mdiag(src5)
+        X = np.vdot(f["dst5"].ravel(), out[:].ravel())
+        assert abs(X - complex(*ref)) / abs(X) < fp["rel_tol"], (tag, X)
+
+
+@pytest.mark.parametrize("prec", ["double", "double_float"])
 def test_gpu_twisted_mass_fingerprint(prec):
     fp = GOLD["fingerprints"]
     dims = fp["grid"]
@@ -129,6 +152,8 @@ WC = dict(mass=0.1, csw_r=1.0, csw_t=1.0, boundary_phases=[1.0, 1.0, 1.0, -1.0])
 WC_ANISO = dict(mass=-0.2, csw_r=1.2, csw_t=0.7, xi_0=1.3, nu=2.1, boundary_phases=[1.0, -1.0, 1j, np.exp(0.3j)])
 MOB = dict(Ls=6, b=1.5, c=0.5, M5=1.8, mass_plus=0.05, mass_minus=0.09, boundary_phases=[1.0, 1.0, 1.0, -1.0])
 TM = dict(mass=0.1, mu=0.3, boundary_phases=[1.0, 1.0, 1.0, -1.0])
+ZMOB = dict(omega=[0.8 + 0.3j, 1.1 - 0.2j, 0.6, 1.4 + 0.1j], b=1.2, c=0.3, M5=1.8, mass=0.07,
+            boundary_phases=[1.0, 1.0, 1.0, -1.0])
 
 
 def _oracle(kind, U, dims, p):
@@ -136,6 +161,8 @@ def _oracle(kind, U, dims, p):
         return o.wilson_clover(U, dims, **p)
     if kind == "wilson_twisted_mass":
         return o.wilson_twisted_mass(U, dims, **p)
+    if kind == "zmobius":
+        return o.zmobius(U, dims, **{k: v for k, v in p.items() if k != "n_rhs"})
     return o.mobius(U, dims, **{k: v for k, v in p.items() if k != "n_rhs"})
 
 
@@ -146,6 +173,7 @@ def _oracle(kind, U, dims, p):
     ("wilson_clover", dict(mass=0.3, boundary_phases=[1, 1, 1, -1]), [2, 2, 2, 2]),
     ("mobius", MOB, [4, 4, 2, 4]),
     ("wilson_twisted_mass", TM, [4, 4, 4, 8]),
+    ("zmobius", ZMOB, [4, 4, 2, 4]),
 ])
 def test_opcodes_vs_oracle(kind, params, dims, prec):
     P = PREC[prec]
@@ -156,7 +184,7 @@ def test_opcodes_vs_oracle(kind, params, dims, prec):
     src_np = rand_field(ref.shape(), 5)
     par = o.parity_of_sites(dims)
     src = to_gpu(op, src_np)
-    for name in ["M", "Mdag", "Mdiag", "Dhop", "DhopDag"] + (["Dminus"] if kind == "mobius" else []):
+    for name in ["M", "Mdag", "Mdiag", "Dhop", "DhopDag"] + (["Dminus", "DminusDag"] if "mobius" in kind else []):
         dst = op.F_lattice()
         op._apply(name, dst, src)
         want = ref.apply(name, src_np)
@@ -173,12 +201,13 @@ def test_opcodes_vs_oracle(kind, params, dims, prec):
 
 
 @pytest.mark.parametrize("prec", ["double", "double_float", "single"])
-def test_mobius_import_export(prec):
+@pytest.mark.parametrize("kind,params", [("mobius", MOB), ("zmobius", ZMOB)])
+def test_mobius_import_export(prec, kind, params):
     P = PREC[prec]
     dims = [4, 4, 4, 4]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 3).U
-    ref = _oracle("mobius", U, dims, MOB)
-    op = gpu_op("mobius", U, dims, P, **MOB)
+    ref = _oracle(kind, U, dims, params)
+    op = gpu_op(kind, U, dims, P, **params)
     s4 = rand_field((ref.V, 4, 3), 1)
     out = op.ImportPhysicalFermionSource(to_gpu(op, s4, five=False))
     assert rel(out[:], ref.import_physical_source(s4)) < TOL[prec]
@@ -218,7 +247,7 @@ def test_multi_rhs_packed_equals_single():
 # ---------------------------------------------------------------------------
 @pytest.mark.parametrize("prec", ["double", "double_float"])
 @pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1)),
-                                         ("wilson_twisted_mass", TM)])
+                                         ("wilson_twisted_mass", TM), ("zmobius", ZMOB)])
 def test_eo2ne_cg_vs_oracle(kind, params, prec):
     dims = [4, 4, 4, 8]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 21).U
