@@ -15,8 +15,14 @@ from .core import (
 from . import _lib
 from . import qcd
 from . import algorithms
+from . import io
+from .io import save, format
 
 
-def load():
-    """Load (building if needed) the native library; raises if unavailable."""
-    return _lib.load()
+def load(path=None):
+    """g.load(path): read a gauge-field file (NERSC format, gpt_gb300.io);
+    g.load() without a path loads (building if needed) the native library and
+    raises if it is unavailable."""
+    if path is None:
+        return _lib.load()
+    return io.load(path)
