@@ -51,6 +51,47 @@ class block_cg(cg):
         raise NotImplementedError("block_cg runs on the device through preconditioned(eo2_ne(), block_cg(...))")
 
 
+class multi_shift_cg:
+    """gpt.algorithms.inverter.multi_shift_cg(eps, maxiter, shifts)
+    (multi_shift_cg.py:51-144): solves (mat + s_j) x_j = src for all shifts
+    with one Krylov space.  Runs on the device for the eo2_ne normal matrix of
+    a native operator (preconditioner.eo2_ne()(op).Mpc); mat(dst_list, src)
+    fills one odd-site half lattice per shift."""
+
+    def __init__(self, params=None, eps=1e-15, maxiter=1000000, shifts=()):
+        p = dict(params or {})
+        self.eps = p.get("eps", eps)
+        self.maxiter = p.get("maxiter", maxiter)
+        self.shifts = [float(s) for s in p.get("shifts", shifts)]
+        self.last = None
+
+    def __call__(self, mat):
+        op = getattr(mat, "native_op", None)
+        if op is None:
+            raise NotImplementedError("multi_shift_cg runs on the device for preconditioner.eo2_ne()(op).Mpc")
+        import ctypes
+
+        from .. import _lib
+        me = self
+
+        def inv(dst, src):
+            n = len(me.shifts)
+            if len(dst) != n:
+                raise ValueError(f"expected {n} destination lattices")
+            sh = (ctypes.c_double * n)(*me.shifts)
+            p = _lib.gbf_cg_params(float(me.eps), int(me.maxiter), 0, 0)
+            r = _lib.gbf_cg_result()
+            _lib.check(_lib.load().gbf_solve_eo2ne_multishift(op.obj, src.ptr, _lib.ptrs([d.ptr for d in dst]), sh, n,
+                                                              ctypes.byref(p), ctypes.byref(r), core.stream_ptr()))
+            for d in dst:
+                d.cb = core.odd
+            me.last = r
+
+        m = _fermion.matrix_operator(inv)
+        m._new_dst = lambda src: [op.F_lattice(core.odd) for _ in me.shifts]
+        return m
+
+
 class preconditioned:
     """M^-1 = L Mpc^-1 R + S (preconditioned.py:28-54)."""
 

@@ -117,6 +117,9 @@ struct gbf_op {
   double2* blk_dev = nullptr;
   double2* blk_host = nullptr;
   long long blk_max_blocks = 0;
+  // multi-shift CG: search directions of the shifts
+  void* ms_mem = nullptr;
+  int ms_count = 0;
 
   size_t half() const { return (size_t)half_bytes(prec, g.N); }
   // workspace half field i; halves 2k and 2k+1 are one contiguous full field,
@@ -416,6 +419,7 @@ void free_op(gbf_op* op) {
   cudaFree(op->partial);
   cudaFree(op->blk_partial);
   cudaFree(op->blk_dev);
+  cudaFree(op->ms_mem);
   if (op->blk_host) cudaFreeHost(op->blk_host);
   cudaFree(op->counter);
   cudaFree(op->st);
@@ -1398,6 +1402,141 @@ extern "C" int gbf_solve_eo2ne_block_cg(gbf_op* op, const void* src, void* x, co
       res->converged = converged;
       res->breakdown = breakdown;
       for (int b = 0; b < k; ++b) res->residual_sq[b] = rel[b];
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// The eo2_ne normal operator and multi-shift CG on it
+// (lib/gpt/algorithms/inverter/multi_shift_cg.py:24-144): solves
+// (Mpc^+ Mpc + s_j) x_j = src on the odd sites for every shift s_j with one
+// Krylov space.  The vector updates run on the device (one fused pass for all
+// shifts); the per-shift scalar recurrences run on the host in double, two
+// reductions read back per iteration, as in the reference.
+// ---------------------------------------------------------------------------
+namespace {
+
+// out = a x + b y on one half field (nrhs 1), then red: 0 none, 2 |out|^2,
+// 3 <x, y> without writing; synchronises s when red != 0 and returns the value
+double blas_half(gbf_op* op, cudaStream_t s, void* out, double a, const void* x, double b, const void* y, int red) {
+  BlasArgs ba{};
+  ba.g = op->g;
+  ba.out = out;
+  ba.x = x;
+  ba.y = y;
+  ba.a_re[0] = a;
+  ba.b_re[0] = b;
+  ba.write = red == 3 ? 0 : 1;
+  ba.red = red;
+  ba.ra = op->red(FIN_STORE);
+  CK(launch_blas(op->prec, ba, s));
+  count_launch();
+  if (!red) return 0.0;
+  double re[kMaxRhs], im[kMaxRhs];
+  read_last(op, s, re, im);
+  return re[0];
+}
+
+}  // namespace
+
+extern "C" int gbf_apply_eo2ne_normal(gbf_op* op, const void* in, void* out, void* stream) {
+  return guarded([&] {
+    if (!op || !in || !out) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    if (in == out) throw Fail(GBF_E_ARG, "source and destination must differ");
+    ensure_ws(op);
+    apply_ne(op, (cudaStream_t)stream, in, out);
+  });
+}
+
+extern "C" int gbf_solve_eo2ne_multishift(gbf_op* op, const void* src, void* const* x, const double* shifts, int n,
+                                          const gbf_cg_params* prm, gbf_cg_result* res, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !x || !shifts || !prm) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    if (n < 1 || n > kMaxShifts) throw Fail(GBF_E_ARG, "1 to 32 shifts");
+    if (op->g.nrhs != 1) throw Fail(GBF_E_UNSUPPORTED, "multi-shift CG takes one right-hand side (n_rhs = 1)");
+    ensure_ws(op);
+    for (int i = 0; i < 8; ++i) op->T(i);
+    const size_t h = op->half();
+    if (op->ms_count < n) {
+      cudaFree(op->ms_mem);
+      op->ms_mem = nullptr;
+      op->ms_mem = dmalloc((size_t)n * h);
+      op->ms_count = n;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int D = GBF_ODD;
+    void *p = op->T(4), *r = op->T(5), *mmp = op->T(6);
+    std::vector<void*> pj(n);
+    for (int j = 0; j < n; ++j) {
+      pj[j] = (char*)op->ms_mem + (size_t)j * h;
+      CK(cudaMemcpyAsync(pj[j], src, h, cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemsetAsync(x[j], 0, h, s));
+    }
+    CK(cudaMemcpyAsync(p, src, h, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(r, src, h, cudaMemcpyDeviceToDevice, s));
+    std::vector<double> rh(n, 1.0), aj(n, 1.0), bj(n, 0.0), gh(n, 1.0);
+    std::vector<int> conv(n, 0);
+    double b = 0.0, a = blas_half(op, s, nullptr, 1.0, src, 0.0, src, 3);
+    if (!(a > 0.0)) throw Fail(GBF_E_ARG, "multi-shift CG needs a non-zero source");
+    const double src2 = a, rsq = prm->eps * prm->eps * a;
+    double cp = a;
+    int iters = 0, breakdown = 0, all = 0;
+    for (int k = 0; k < prm->maxiter && !all; ++k) {
+      const double c = cp;
+      // mmp = Mpc^+ Mpc p, d = Re <p, mmp>
+      void *t = op->T(0), *z = op->T(1), *w = op->T(2), *u = op->T(3);
+      op->local(s, D, p, t, op->G());
+      op->dslash(s, GBF_EVEN, false, t, z, op->G());
+      op->dslash(s, D, false, z, w, op->none(), -1.0, p, 1.0);
+      op->dslash(s, GBF_EVEN, true, w, u, op->Gdag());
+      op->dslash(s, D, true, u, mmp, op->Gdag(), -1.0, w, 1.0, op->none(), 1, p, FIN_STORE);
+      double dre[kMaxRhs], dim[kMaxRhs];
+      read_last(op, s, dre, dim);
+      const double d = dre[0];
+      if (!(d > 0.0) || !std::isfinite(d)) {
+        breakdown = 1;
+        break;
+      }
+      double om = b / a;
+      a = c / d;
+      om *= a;
+      cp = blas_half(op, s, r, -a, mmp, 1.0, r, 2);  // r -= a mmp ; |r|^2
+      b = cp / c;
+      MultiShiftArgs ms{};
+      ms.r = r;
+      for (int j = 0; j < n; ++j) {
+        if (conv[j]) continue;
+        const double q = 1.0 / (1.0 + shifts[j] * a + (1.0 - rh[j]) * om);
+        rh[j] = q;
+        aj[j] = q * a;
+        bj[j] = q * q * b;
+        gh[j] *= q;
+        ms.x[ms.n] = x[j];
+        ms.p[ms.n] = pj[j];
+        ms.a[ms.n] = aj[j];
+        ms.b[ms.n] = bj[j];
+        ms.g[ms.n] = gh[j];
+        ++ms.n;
+      }
+      CK(launch_multishift(op->prec, op->g, ms, s));
+      count_launch();
+      blas_half(op, s, p, b, p, 1.0, r, 0);  // p = b p + r
+      iters = k + 1;
+      all = 1;
+      for (int j = 0; j < n; ++j) {
+        if (!conv[j] && gh[j] * gh[j] * cp <= rsq) conv[j] = 1;
+        all &= conv[j];
+      }
+    }
+    CK(cudaStreamSynchronize(s));
+    if (res) {
+      std::memset(res, 0, sizeof(*res));
+      res->iterations = iters;
+      res->converged = all;
+      res->breakdown = breakdown;
+      for (int j = 0; j < n && j < 16; ++j) res->residual_sq[j] = gh[j] * gh[j] * cp / src2;
     }
   });
 }

@@ -319,3 +319,52 @@ cudaError_t launch_lincomb(int P, const Geo& g, void* out, const void* Y, double
 }
 
 }  // namespace gbf
+
+namespace gbf {
+
+// Multi-shift CG vector update for the active shifts j (one pass over r):
+//   x_j += a_j p_j ;  p_j = b_j p_j + g_j r
+// (lib/gpt/algorithms/inverter/multi_shift_cg.py:45-47).  bytes/site: r once,
+// x_j and p_j read and written per active shift.
+template <int P>
+__global__ void __launch_bounds__(256) multishift_kernel(const Geo g, const MultiShiftArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
+    V r[12];
+    load_spinor<P>(a.r, g.N, n, r);
+    for (int j = 0; j < a.n; ++j) {
+      V x[12], p[12];
+      load_spinor<P>(a.x[j], g.N, n, x);
+      load_spinor<P>(a.p[j], g.N, n, p);
+      const R aj = (R)a.a[j], bj = (R)a.b[j], gj = (R)a.g[j];
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        x[k] = mk<R>(fma(aj, p[k].x, x[k].x), fma(aj, p[k].y, x[k].y));
+        p[k] = mk<R>(fma(bj, p[k].x, gj * r[k].x), fma(bj, p[k].y, gj * r[k].y));
+      }
+      store_spinor<P>(a.x[j], g.N, n, x);
+      store_spinor<P>(a.p[j], g.N, n, p);
+    }
+  }
+}
+
+cudaError_t launch_multishift(int P, const Geo& g, const MultiShiftArgs& a, cudaStream_t st) {
+  if (a.n < 0 || a.n > kMaxShifts) return cudaErrorInvalidValue;
+  if (a.n == 0) return cudaSuccess;
+  const int bd = 256;
+  const void* k = P == P64 ? (const void*)multishift_kernel<P64>
+                : P == P32 ? (const void*)multishift_kernel<P32>
+                : P == P16 ? (const void*)multishift_kernel<P16>
+                : P == PDD ? (const void*)multishift_kernel<PDD> : nullptr;
+  if (!k) return cudaErrorInvalidValue;
+  const long long nb = reduce_grid((g.N + bd - 1) / bd, 1, resident_blocks(k, bd, 0));
+  if (P == P64) multishift_kernel<P64><<<(unsigned)nb, bd, 0, st>>>(g, a);
+  else if (P == P32) multishift_kernel<P32><<<(unsigned)nb, bd, 0, st>>>(g, a);
+  else if (P == P16) multishift_kernel<P16><<<(unsigned)nb, bd, 0, st>>>(g, a);
+  else multishift_kernel<PDD><<<(unsigned)nb, bd, 0, st>>>(g, a);
+  return cudaGetLastError();
+}
+
+}  // namespace gbf

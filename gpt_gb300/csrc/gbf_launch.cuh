@@ -109,6 +109,17 @@ cudaError_t launch_gram(int P, const Geo& g, const void* A, const void* B, doubl
                         unsigned* counter, double2* out, cudaStream_t st);
 cudaError_t launch_lincomb(int P, const Geo& g, void* out, const void* Y, double beta, const void* X, const double2* W,
                            cudaStream_t st);
+// multi-shift CG update over the active shifts: x_j += a_j p_j ; p_j = b_j p_j + g_j r
+constexpr int kMaxShifts = 32;
+struct MultiShiftArgs {
+  const void* r;
+  void* x[kMaxShifts];
+  void* p[kMaxShifts];
+  double a[kMaxShifts], b[kMaxShifts], g[kMaxShifts];
+  int n;
+};
+cudaError_t launch_multishift(int P, const Geo& g, const MultiShiftArgs& a, cudaStream_t st);
+
 // out1 = b1 Y1 + X1 W1 ; out2 = b2 Y2 + c out1 + X2 W2 in one pass
 cudaError_t launch_lincomb2(int P, const Geo& g, void* out1, const void* Y1, double b1, const void* X1, const double2* W1,
                             void* out2, const void* Y2, double b2, double c, const void* X2, const double2* W2,

@@ -339,6 +339,21 @@ class preconditioner:
 
 
 class _eo2_ne_matrix:
+    """The eo2_ne-preconditioned system of `op`; `Mpc` is the normal matrix
+    Mpc^+ Mpc on half lattices of the odd sites
+    (lib/gpt/algorithms/preconditioner/normal_equation.py:35-65), applied by
+    gbf_apply_eo2ne_normal."""
+
     def __init__(self, op, parity):
         self.op = op
         self.parity = parity
+
+        def _ne(dst, src):
+            if src.cb is not core.odd:
+                raise ValueError("Mpc acts on odd-site half lattices")
+            _lib.check(_lib.load().gbf_apply_eo2ne_normal(op.obj, src.ptr, dst.ptr, core.stream_ptr()))
+            dst.cb = core.odd
+
+        self.Mpc = matrix_operator(_ne, _ne)
+        self.Mpc._new_dst = lambda src: op.F_lattice(core.odd)
+        self.Mpc.native_op = op

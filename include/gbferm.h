@@ -163,6 +163,18 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
 int gbf_solve_eo2ne_block_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* p, gbf_cg_result* res,
                              void* stream);
 
+/* The eo2_ne normal operator Mpc^+ Mpc on odd-site half fields (the matrix
+ * the eo2_ne CG inverts, lib/gpt/algorithms/preconditioner/normal_equation.py
+ * over schur_complement_two.py), and multi-shift CG on it
+ * (lib/gpt/algorithms/inverter/multi_shift_cg.py:24-144): x[j] (n half
+ * fields) receive the solutions of (Mpc^+ Mpc + shifts[j]) x_j = src for
+ * n <= 32 shifts >= 0, n_rhs = 1.  Converged when every shift's recursive
+ * residual satisfies |r_j|^2 <= eps^2 |src|^2; residual_sq[j] (j < 16) gets
+ * that ratio. */
+int gbf_apply_eo2ne_normal(gbf_op* op, const void* in, void* out, void* stream);
+int gbf_solve_eo2ne_multishift(gbf_op* op, const void* src, void* const* x, const double* shifts, int n,
+                               const gbf_cg_params* p, gbf_cg_result* res, void* stream);
+
 /* Autotuner (the role of lib/gpt/core/auto_tune.py for this library): times
  * the block-size candidates of the four kernel classes -- [0] hopping kernel
  * with a per-thread epilogue, [1] hopping kernel with the Mobius s-matrix
