@@ -1,6 +1,6 @@
 """CPU oracle for the gpt fermion-matrix hot path -- TEST INFRASTRUCTURE ONLY.
 
-This package is the checker for the CUDA path in ``gpt_gb300``.  Only
+This package is the oracle for the CUDA path in ``gpt_gb300``.  Only
 ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline / reference leg of
 ``bench.py`` may import it; the product never does.
 

@@ -1,6 +1,6 @@
 // oracle.cpp -- CPU restatement of the gpt fermion-matrix hot path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path in
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle for the CUDA path in
 // gpt_gb300/csrc: tests/, __graft_entry__.smoke() and the cpu_baseline /
 // reference leg of bench.py may load it; the product never does.
 //
