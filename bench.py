@@ -742,11 +742,17 @@ def run_gbf(args, dims):
 
     # ---- CPU baseline (oracle port), rank 0 at N = 1 only ----
     cpu = None
+    oracle_res = {}
     if world == 1 and not args.no_cpu_baseline:
         import oracle as o
 
         op_o = o.wilson_clover(U.U, dims, mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"],
                                boundary_phases=CFG["phases"], with_single=True)
+        # FP64 oracle residual of the mixed and the plain solutions
+        for name, sol in (("mixed", x), ("plain", xp)):
+            xs = sol[:]
+            rr = src_np - op_o.apply("M", xs)
+            oracle_res[name] = math.sqrt(o.norm2(rr) / o.norm2(src_np))
         per_iter, t_m, spent = cpu_sample_rates(op_o, src_np)
         sec = inner_iters_per_solve * per_iter + (outer_iters + 1) * t_m
         cpu = {"value": 1.0 / sec, "unit": "solves/s", "cores": o.num_threads(), "kind": "port",
@@ -781,10 +787,10 @@ def run_gbf(args, dims):
         "cpu_baseline": cpu,
         "p50_ms": p[len(p) // 2],
         "p99_ms": p[min(len(p) - 1, int(math.ceil(0.99 * len(p))) - 1)],
-        "mixed": {"solves_per_s": value, "true_residual": true_res, "outer_corrections": outer_iters,
-                  "inner_cg_iterations": inner_iters_per_solve},
+        "mixed": {"solves_per_s": value, "true_residual": true_res, "true_residual_oracle": oracle_res.get("mixed"),
+                  "outer_corrections": outer_iters, "inner_cg_iterations": inner_iters_per_solve},
         "plain_fp64": {"solves_per_s": world * 1000.0 / plain_ms, "ms_per_solve": plain_ms, "cg_iterations": plain_it,
-                       "true_residual": plain_true},
+                       "true_residual": plain_true, "true_residual_oracle": oracle_res.get("plain")},
         "mixed_over_plain": (value / world) / (1000.0 / plain_ms),
         "dslash_fp32": {"hbm_gbs": achieved, "avg_launch_ms": d_ms},
         "dslash_fp64": {"algorithmic_gbs": fp64_gbs, "avg_launch_ms": d64_ms, "frac_of_hbm_peak": fp64_gbs / peak,
