@@ -106,8 +106,15 @@ struct gbf_op {
   unsigned* errbits = nullptr;
   cudaStream_t stream = nullptr; // internal stream for graph capture
   cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_chk[2] = {nullptr, nullptr};
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;   // K CG iterations (host-checked loop)
   int graph_K = 0;
+  cudaGraphExec_t cgraph = nullptr;  // the whole CG loop: a conditional while node
+  unsigned long long cond = 0;       // its loop condition
+  bool cond_active = false;          // set while the loop body is captured
+  void drop_graphs() {
+    if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+    if (cgraph) { cudaGraphExecDestroy(cgraph); cgraph = nullptr; }
+  }
   // block sizes chosen by gbf_tune (0: default): hop with a per-thread
   // epilogue, hop with the s-matrix epilogue, site-local kernel, CG update
   int tuned_bd[4] = {0, 0, 0, 0};
@@ -229,6 +236,8 @@ struct gbf_op {
     a.x = x;
     a.p = p;
     a.ra = red(FIN_BETA);
+    a.ra.cond = cond;
+    a.ra.use_cond = cond_active ? 1 : 0;
     a.bd = tuned_bd[3];
     CK(launch_cg_update(prec, a, s));
     count_launch();
@@ -411,7 +420,7 @@ void ensure_ws(gbf_op* op) {
 }
 
 void free_op(gbf_op* op) {
-  if (op->graph) cudaGraphExecDestroy(op->graph);
+  op->drop_graphs();
   cudaFree(op->links);
   cudaFree(op->clov_mem);
   cudaFree(op->smat);
@@ -547,7 +556,7 @@ int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus) {
     op->par.mass_plus = mass_plus;
     op->par.mass_minus = mass_minus;
     build_smat(op);
-    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+    op->drop_graphs();
   });
 }
 
@@ -667,7 +676,7 @@ static void update_gauge_impl(gbf_op* op, const void* U, int on_device, const gb
       cudaFree(tmpU);
     }
     op->gauge_set = true;
-    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+    op->drop_graphs();
   }
 }
 
@@ -1018,10 +1027,56 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
       }
       for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
     }
-    // ---- CG loop in graphs of K iterations ----
+    bool device_loop = false;
+    if (!prm->profile && prm->iterations_per_graph <= 0) {
+      // ---- the whole CG loop on the device: a conditional while node whose
+      // body is one iteration; the CG update kernel sets the loop condition to
+      // !all_done (converged, maxiter reached or every rhs broken down), and
+      // its early exit sets it to 0, so the loop ends within maxiter + 1
+      // bodies.  No host round trip and no iteration past convergence. ----
+      device_loop = true;
+      if (!op->cgraph) {
+        cudaGraph_t gr;
+        CK(cudaGraphCreate(&gr, 0));
+        try {
+          cudaGraphConditionalHandle h;
+          CK(cudaGraphConditionalHandleCreate(&h, gr, 1, cudaGraphCondAssignDefault));
+          cudaGraphNodeParams np{};
+          np.type = cudaGraphNodeTypeConditional;
+          np.conditional.handle = h;
+          np.conditional.type = cudaGraphCondTypeWhile;
+          np.conditional.size = 1;
+          cudaGraphNode_t node;
+          CK(cudaGraphAddNode(&node, gr, nullptr, nullptr, 0, &np));
+          cudaGraph_t body = np.conditional.phGraph_out[0];
+          CK(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+          op->cond = h;
+          op->cond_active = true;
+          try {
+            cg_iteration(op, s);
+          } catch (...) {
+            op->cond_active = false;
+            cudaGraph_t t;
+            cudaStreamEndCapture(s, &t);
+            throw;
+          }
+          op->cond_active = false;
+          cudaGraph_t t;
+          CK(cudaStreamEndCapture(s, &t));
+          CK(cudaGraphInstantiate(&op->cgraph, gr, 0));
+        } catch (...) {
+          cudaGraphDestroy(gr);
+          throw;
+        }
+        cudaGraphDestroy(gr);
+      }
+      CK(cudaGraphLaunch(op->cgraph, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    // ---- CG loop in graphs of K iterations, convergence checked by the host ----
     const int K = prm->iterations_per_graph > 0 ? prm->iterations_per_graph : 8;
-    if (!prm->profile && (!op->graph || op->graph_K != K)) {
-      if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+    if (!prm->profile && !device_loop && (!op->graph || op->graph_K != K)) {
+      op->drop_graphs();
       cudaGraph_t gr;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
@@ -1035,7 +1090,7 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
       cudaGraphDestroy(gr);
       op->graph_K = K;
     }
-    const int max_launches = prm->profile ? 0 : (prm->maxiter + K - 1) / K;
+    const int max_launches = (prm->profile || device_loop) ? 0 : (prm->maxiter + K - 1) / K;
     bool done = false;
     int launched = 0;
     for (; launched < max_launches && !done; ++launched) {
@@ -1059,6 +1114,7 @@ int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params
     CK(cudaStreamWaitEvent(user, op->ev_out, 0));
     CK(cudaEventSynchronize(op->ev_out));
     const CGState& st = op->hst[0];
+    if (device_loop) count_launch((unsigned long long)(st.iter > 0 ? st.iter : 1) * kKernelsPerIteration);
     if (res) {
       res->iterations = st.iter;
       int conv = 1;
@@ -1143,7 +1199,7 @@ int gbf_tune(gbf_op* op, void* stream, int* out_bd, double* out_us) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+    op->drop_graphs();
   });
 }
 
@@ -1151,7 +1207,7 @@ int gbf_set_tuning(gbf_op* op, const int* bd) {
   return guarded([&] {
     if (!op || !bd) throw Fail(GBF_E_ARG, "null argument");
     for (int i = 0; i < 4; ++i) op->tuned_bd[i] = bd[i] > 0 ? pick_bd(bd[i], op->g.N5) : 0;
-    if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+    op->drop_graphs();
   });
 }
 

@@ -342,6 +342,10 @@ struct RedArgs {
   double2* partial;   // [gridDim][nrhs]
   unsigned* counter;  // zero on entry, restored to zero by the last block
   CGState* st;
+  // FIN_BETA inside a conditional while graph: the last block sets the loop
+  // condition to !all_done (all_done also covers maxiter and breakdown)
+  unsigned long long cond;
+  int use_cond;
 };
 
 __device__ __forceinline__ void finalize(const RedArgs& r, int rhs, double re, double im) {
@@ -489,6 +493,7 @@ __device__ __forceinline__ void block_reduce_finalize(const RedArgs& r, double v
         if (r.st->iter >= r.st->maxiter) all = 1;
       }
       r.st->all_done = all;
+      if (r.fin == FIN_BETA && r.use_cond) cudaGraphSetConditional(r.cond, all ? 0u : 1u);
     }
     *r.counter = 0;
     __threadfence();

@@ -142,7 +142,11 @@ __global__ void __launch_bounds__(256) cg_update_kernel(const CGUpdateArgs a) {
   using V = cplx<R>;
   extern __shared__ __align__(16) double smem_d[];
   const Geo& g = a.g;
-  if (a.ra.st->all_done) return;
+  if (a.ra.st->all_done) {
+    // every execution of the CG loop's last kernel sets the loop condition
+    if (a.ra.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.ra.cond, 0u);
+    return;
+  }
   double vr = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {

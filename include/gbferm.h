@@ -130,12 +130,14 @@ int gbf_convert(gbf_op* dst_op, void* dst, gbf_op* src_op, const void* src, doub
  * (lib/gpt/algorithms/inverter/preconditioned.py:32-54, cg.py:47-105,
  * lib/gpt/qcd/fermion/preconditioner/even_odd_sites.py:61-72): solves
  * M x = src for all packed right-hand sides with zero initial guess.  The CG
- * loop runs in CUDA graphs with device-resident scalars; the host checks
- * convergence once per graph launch. */
+ * loop runs in a CUDA graph with device-resident scalars (see
+ * iterations_per_graph). */
 typedef struct {
   double eps;
   int maxiter;
-  int iterations_per_graph; /* 0: default */
+  int iterations_per_graph; /* 0: the whole CG loop runs on the device (a CUDA graph with a
+                               conditional while node, no host round trip); K > 0: graphs of K
+                               iterations, convergence checked by the host between them */
   int profile;              /* 1: no graphs; CUDA events time every kernel class (diagnostic run) */
 } gbf_cg_params;
 typedef struct {

@@ -363,6 +363,27 @@ def test_reductions_bitwise_deterministic():
     assert n1 == n2
 
 
+@pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1))])
+def test_device_loop_equals_host_checked_graphs(kind, params):
+    """The CG loop as one conditional-while graph (default) and as host-checked
+    graphs of 8 iterations run the same kernels: bitwise equal solutions and
+    the same iteration count."""
+    dims = [4, 4, 4, 8]
+    U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 33).U
+    op = gpu_op(kind, U, dims, g.double, **params)
+    b = to_gpu(op, rand_field(op.F_lattice()[:].shape, 3))
+    inv = g.algorithms.inverter
+    pc = g.qcd.fermion.preconditioner
+    out = []
+    for K in (0, 8, 0):
+        cg = inv.cg({"eps": 1e-10, "maxiter": 2000, "iterations_per_graph": K})
+        x = inv.preconditioned(pc.eo2_ne(), cg)(op)(b)
+        assert cg.last.converged
+        out.append((cg.last.iterations, x[:]))
+    assert out[0][0] == out[1][0] == out[2][0]
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][1], out[2][1])
+
+
 def test_cg_maxiter_reports_not_converged():
     dims = [4, 4, 4, 4]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.3, 6).U
