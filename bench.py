@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--rhs-group", type=int, default=0, help="c4: right-hand sides solved together (0: auto)")
     ap.add_argument("--with-plain", action="store_true",
                     help="c3: also time one plain FP64 and one plain double-float packed solve of the same sources")
+    ap.add_argument("--cg-graph", type=int, default=0,
+                    help="c2: CG iterations per CUDA graph with a host convergence check between graphs "
+                         "(0: the whole CG loop on the device, one graph with a conditional while node; -1: no "
+                         "graphs, every kernel launched from the host, for per-kernel launch lists under ncu)")
     ap.add_argument("--solver", default="cg", choices=["cg", "block_cg"],
                     help="c3/c4 inner solver: independent CG per packed rhs, or block CG over them")
     return ap.parse_args()
@@ -566,14 +570,15 @@ def run_gbf(args, dims):
     op = g.qcd.fermion.wilson_clover(U, params)
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
-    inner_cg = inv.cg({"eps": CFG["inner_tol"], "maxiter": 20000})
+    cg_loop = {"iterations_per_graph": max(0, args.cg_graph), "profile": args.cg_graph < 0}
+    inner_cg = inv.cg({"eps": CFG["inner_tol"], "maxiter": 20000, **cg_loop})
     dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inner_cg), g.single, g.double),
                                eps=CFG["tol"], maxiter=100)
     solver = dc(op)
     inner_op = dc.inner_inverter.inner_op  # the FP32 operator built by mixed_precision
     # the plain CG's eps bounds the eo2_ne normal residual; tol / 3 brings the
     # true residual of M x = b below tol (eps = tol leaves it at 1.5 tol)
-    plain_cg = inv.cg({"eps": CFG["tol"] / 3, "maxiter": 40000})
+    plain_cg = inv.cg({"eps": CFG["tol"] / 3, "maxiter": 40000, **cg_loop})
     plain = inv.preconditioned(pc.eo2_ne(), plain_cg)(op)
 
     V = grid.gsites
@@ -794,6 +799,9 @@ def run_gbf(args, dims):
         "plain_fp64": {"solves_per_s": world * 1000.0 / plain_ms, "ms_per_solve": plain_ms, "cg_iterations": plain_it,
                        "true_residual": plain_true, "true_residual_oracle": oracle_res.get("plain")},
         "mixed_over_plain": (value / world) / (1000.0 / plain_ms),
+        "cg_loop": ("device: one CUDA graph with a conditional while node" if args.cg_graph == 0 else
+                    f"host-checked CUDA graphs of {args.cg_graph} iterations" if args.cg_graph > 0 else
+                    "no graphs: host launches with CUDA events (diagnostic)"),
         "dslash_fp32": {"hbm_gbs": achieved, "avg_launch_ms": d_ms},
         "dslash_fp64": {"algorithmic_gbs": fp64_gbs, "avg_launch_ms": d64_ms, "frac_of_hbm_peak": fp64_gbs / peak,
                         "gflops_model_1320_per_site": 1320 * Vh / (d64_ms / 1000.0) / 1e9,

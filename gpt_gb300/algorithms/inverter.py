@@ -17,18 +17,25 @@ class cg:
     """gpt.algorithms.inverter.cg(eps, maxiter): CG on the eo2_ne normal
     equations; convergence when |r|^2 <= eps^2 |b|^2 (cg.py:70, 103)."""
 
-    def __init__(self, params=None, eps=1e-15, maxiter=1000000, fail_if_not_converged=False, iterations_per_graph=0):
+    def __init__(self, params=None, eps=1e-15, maxiter=1000000, fail_if_not_converged=False, iterations_per_graph=0,
+                 profile=False):
         p = dict(params or {})
         self.eps = p.get("eps", eps)
         self.maxiter = p.get("maxiter", maxiter)
         self.fail_if_not_converged = p.get("fail_if_not_converged", fail_if_not_converged)
+        # iterations_per_graph 0: the whole CG loop runs on the device (one CUDA
+        # graph with a conditional while node); K > 0: graphs of K iterations
+        # with a host convergence check between them.  profile: no graphs,
+        # every kernel launched from the host between CUDA events (diagnostic)
         self.iterations_per_graph = p.get("iterations_per_graph", iterations_per_graph)
+        self.profile = bool(p.get("profile", profile))
         self.history = []
         self.last = None
         self.total_iterations = 0
 
     def modified(self, **params):
-        d = dict(eps=self.eps, maxiter=self.maxiter, fail_if_not_converged=self.fail_if_not_converged)
+        d = dict(eps=self.eps, maxiter=self.maxiter, fail_if_not_converged=self.fail_if_not_converged,
+                 iterations_per_graph=self.iterations_per_graph, profile=self.profile)
         d.update(params)
         return cg(d)
 
@@ -111,7 +118,7 @@ class preconditioned:
         solve = op._solve_eo2ne_block_cg if isinstance(inv, block_cg) else op._solve_eo2ne_cg
 
         def mat(dst, src):
-            r = solve(dst, src, inv.eps, inv.maxiter, inv.iterations_per_graph)
+            r = solve(dst, src, inv.eps, inv.maxiter, inv.iterations_per_graph, int(inv.profile))
             inv.last = r
             inv.history = [None] * r.iterations
             inv.total_iterations += r.iterations

@@ -365,9 +365,9 @@ def test_reductions_bitwise_deterministic():
 
 @pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1))])
 def test_device_loop_equals_host_checked_graphs(kind, params):
-    """The CG loop as one conditional-while graph (default) and as host-checked
-    graphs of 8 iterations run the same kernels: bitwise equal solutions and
-    the same iteration count."""
+    """The CG loop as one conditional-while graph (default), as host-checked
+    graphs of 8 iterations and as plain host launches (profile) runs the same
+    kernels: bitwise equal solutions and the same iteration count."""
     dims = [4, 4, 4, 8]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 33).U
     op = gpu_op(kind, U, dims, g.double, **params)
@@ -375,13 +375,13 @@ def test_device_loop_equals_host_checked_graphs(kind, params):
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
     out = []
-    for K in (0, 8, 0):
-        cg = inv.cg({"eps": 1e-10, "maxiter": 2000, "iterations_per_graph": K})
+    for K, prof in ((0, False), (8, False), (0, False), (0, True)):
+        cg = inv.cg({"eps": 1e-10, "maxiter": 2000, "iterations_per_graph": K, "profile": prof})
         x = inv.preconditioned(pc.eo2_ne(), cg)(op)(b)
         assert cg.last.converged
         out.append((cg.last.iterations, x[:]))
-    assert out[0][0] == out[1][0] == out[2][0]
-    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][1], out[2][1])
+    assert len({o[0] for o in out}) == 1
+    assert all(np.array_equal(out[0][1], o[1]) for o in out[1:])
 
 
 def test_cg_maxiter_reports_not_converged():
