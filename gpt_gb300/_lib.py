@@ -99,6 +99,10 @@ def load():
         "gbf_solve_eo2ne_block_cg": (I, [P, P, P, ctypes.POINTER(gbf_cg_params), ctypes.POINTER(gbf_cg_result), P]),
         "gbf_apply_eo2ne_normal": (I, [P, P, P, P]),
         "gbf_solve_eo2ne_multishift": (I, [P, P, PP, DP, I, ctypes.POINTER(gbf_cg_params), ctypes.POINTER(gbf_cg_result), P]),
+        "gbf_solve_normal_cg": (I, [P, P, P, ctypes.POINTER(gbf_cg_params), ctypes.POINTER(gbf_cg_result), P]),
+        "gbf_eo2ne_prepare": (I, [P, P, P, P]),
+        "gbf_eo2ne_reconstruct": (I, [P, P, P, P, P]),
+        "gbf_modes_apply": (I, [P, PP, PP, DP, I, P, P, I, P]),
         "gbf_last_error": (ctypes.c_char_p, []),
         "gbf_stream_sync": (I, [P]),
         "gbf_launch_count": (ctypes.c_ulonglong, []),

@@ -1,1 +1,1 @@
-from . import inverter
+from . import inverter, modes

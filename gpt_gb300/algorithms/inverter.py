@@ -1,6 +1,8 @@
 """Krylov inverters of the hot path: cg, preconditioned, defect_correcting,
 mixed_precision (lib/gpt/algorithms/inverter/cg.py:24-117,
-preconditioned.py:24-54, defect_correcting.py:23-142, mixed_precision.py:23-32).
+preconditioned.py:24-54, defect_correcting.py:23-142, mixed_precision.py:23-32),
+and the adjacent solver layers block_cg, multi_shift_cg, deflate and
+sequence (block_cg.py, multi_shift_cg.py, deflate.py, sequence.py).
 
 preconditioned(eo2_ne(), cg(...)) on a native fermion operator runs as one
 device-resident solve (prepare, CG in CUDA graphs, reconstruction) through
@@ -40,7 +42,38 @@ class cg:
         return cg(d)
 
     def __call__(self, mat):
-        raise NotImplementedError("cg runs on the device through preconditioned(eo2_ne(), cg(...))")
+        """cg(mat) for the eo2_ne normal operator of a native operator
+        (preconditioner.eo2_ne()(op).Mpc): CG on the device starting from the
+        destination as the guess (gbf_solve_normal_cg; the reference's
+        guess handling, cg.py:48-68: r = src - mat psi, zero source -> zero
+        solution).  A guess that already meets the tolerance returns after
+        zero iterations."""
+        op = getattr(mat, "native_op", None)
+        if op is None:
+            raise NotImplementedError("cg runs on the device for preconditioner.eo2_ne()(op).Mpc or through "
+                                      "preconditioned(eo2_ne(), cg(...))")
+        import ctypes
+
+        from .. import _lib
+        me = self
+
+        def inv(dst, src):
+            if src.cb is not core.odd or dst.cb is not core.odd:
+                raise ValueError("the eo2_ne normal operator acts on odd-site half lattices")
+            p = _lib.gbf_cg_params(float(me.eps), int(me.maxiter), int(me.iterations_per_graph), int(me.profile))
+            r = _lib.gbf_cg_result()
+            _lib.check(_lib.load().gbf_solve_normal_cg(op.obj, src.ptr, dst.ptr, ctypes.byref(p), ctypes.byref(r),
+                                                       core.stream_ptr()))
+            me.last = r
+            me.history = [None] * r.iterations
+            me.total_iterations += r.iterations
+            if me.fail_if_not_converged and not r.converged:
+                raise ValueError("FATAL error: CG not converged")
+
+        m = _fermion.matrix_operator(inv, inv_mat=mat.mat)
+        m._new_dst = lambda src: op.F_lattice(core.odd)
+        m.accept_guess = True
+        return m
 
 
 class block_cg(cg):
@@ -99,6 +132,46 @@ class multi_shift_cg:
         return m
 
 
+class deflate:
+    """gpt.algorithms.inverter.deflate(evec, ev) (deflate.py:23-32): the
+    low-mode part sum_n evec_n evec_n^+ / ev_n of the inverse, as a mode
+    matrix applied on the device (algorithms.modes.matrix).  Used alone it is
+    the low-mode approximation; in sequence(deflate(...), cg(...)) it is the
+    guess from which the CG starts."""
+
+    def __init__(self, evec, ev, params=None, block=16):
+        self.evec = list(evec)
+        self.ev = [float(x) if complex(x).imag == 0 else complex(x) for x in ev]
+        self.block = (params or {}).get("block", block)
+
+    def __call__(self, matrix):
+        from . import modes
+        m = modes.matrix(self.evec, self.evec, self.ev, lambda x: 1.0 / x, block=self.block)
+        m.accept_guess = False
+        return m
+
+
+class sequence:
+    """gpt.algorithms.inverter.sequence(*inverters) (sequence.py:23-42): the
+    inverters of one matrix applied in turn to the same (dst, src), each
+    later one starting from the result of the one before."""
+
+    def __init__(self, *inverters):
+        self.inverters = inverters
+
+    def __call__(self, outer_mat):
+        mats = [i(outer_mat) for i in self.inverters]
+
+        def inv(dst, src):
+            for m in mats:
+                m(dst, src)
+
+        m = _fermion.matrix_operator(inv, inv_mat=getattr(outer_mat, "mat", None))
+        m._new_dst = mats[0]._new_dst
+        m.accept_guess = True
+        return m
+
+
 class preconditioned:
     """M^-1 = L Mpc^-1 R + S (preconditioned.py:28-54)."""
 
@@ -107,13 +180,15 @@ class preconditioned:
         self.inverter = inverter
 
     def __call__(self, op):
-        if not isinstance(self.preconditioner, _fermion.preconditioner.eo2_ne) or not isinstance(self.inverter, cg):
-            raise NotImplementedError("the device path implements preconditioned(eo2_ne(), cg(...) or block_cg(...))")
+        if not isinstance(self.preconditioner, _fermion.preconditioner.eo2_ne):
+            raise NotImplementedError("the device path implements the eo2_ne preconditioner")
         if not isinstance(op, _fermion.fermion_operator):
             raise TypeError("expected a native fermion operator")
         if op.daggered:
             raise NotImplementedError("solves with the daggered operator are not on this path")
         inv = self.inverter
+        if not isinstance(inv, cg):
+            return self._composed(op)
 
         solve = op._solve_eo2ne_block_cg if isinstance(inv, block_cg) else op._solve_eo2ne_cg
 
@@ -130,6 +205,26 @@ class preconditioned:
 
         m = _fermion.matrix_operator(mat, inv_mat=op.mat)
         m._new_dst = new_dst
+        return m
+
+    def _composed(self, op):
+        """L Mpc^-1 R + S around any inverter of the normal operator (for
+        example sequence(deflate(...), cg(...))): R and L S on the device
+        (gbf_eo2ne_prepare / gbf_eo2ne_reconstruct), the inverter on
+        preconditioner.eo2_ne()(op).Mpc with a zero guess."""
+        from .. import _lib
+        inner = self.inverter(self.preconditioner(op).Mpc)
+
+        def mat(dst, src):
+            b = op.F_lattice(core.odd)
+            _lib.check(_lib.load().gbf_eo2ne_prepare(op.obj, src.ptr, b.ptr, core.stream_ptr()))
+            y = op.F_lattice(core.odd)
+            inner(y, b)
+            _lib.check(_lib.load().gbf_eo2ne_reconstruct(op.obj, src.ptr, y.ptr, dst.ptr, core.stream_ptr()))
+            dst.cb = core.full
+
+        m = _fermion.matrix_operator(mat, inv_mat=op.mat)
+        m._new_dst = lambda src: op.F_lattice()
         return m
 
 

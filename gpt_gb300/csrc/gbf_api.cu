@@ -127,6 +127,10 @@ struct gbf_op {
   // multi-shift CG: search directions of the shifts
   void* ms_mem = nullptr;
   int ms_count = 0;
+  // reduction partials: capacity of `partial` in double2 entries
+  long long partial_cap = 0;
+  // mode representation: inner products of one block of modes (device)
+  double2* mode_dev = nullptr;
 
   size_t half() const { return (size_t)half_bytes(prec, g.N); }
   // workspace half field i; halves 2k and 2k+1 are one contiguous full field,
@@ -407,6 +411,7 @@ void ensure_ws(gbf_op* op) {
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long maxblocks = std::min<long long>(op->g.Vh + 1, (long long)sms * 32 + 4096);
   op->partial = (double2*)dmalloc((size_t)maxblocks * op->g.nrhs * sizeof(double2));
+  op->partial_cap = maxblocks * op->g.nrhs;
   op->counter = (unsigned*)dmalloc(sizeof(unsigned) * 4);
   CK(cudaMemset(op->counter, 0, sizeof(unsigned) * 4));
   op->st = (CGState*)dmalloc(sizeof(CGState));
@@ -429,6 +434,7 @@ void free_op(gbf_op* op) {
   cudaFree(op->blk_partial);
   cudaFree(op->blk_dev);
   cudaFree(op->ms_mem);
+  cudaFree(op->mode_dev);
   if (op->blk_host) cudaFreeHost(op->blk_host);
   cudaFree(op->counter);
   cudaFree(op->st);
@@ -975,159 +981,346 @@ int gbf_apply(gbf_op* op, int opcode, const void* const* src, void* const* dst, 
   });
 }
 
+}  // extern "C"
+
+namespace {
+
+void apply_ne(gbf_op* op, cudaStream_t s, const void* in, void* out);
+
+// R_ne of the eo2_ne system: b = Mpc^+ (src_D - Dhop G_C src_C) on the odd
+// sites (normal_equation.py:47-48, schur_complement_two.py:87-104); with
+// norm = true |b|^2 goes to the CG state (FIN_STORE, the `last` slot)
+void eo2ne_prepare(gbf_op* op, cudaStream_t s, const void* src, void* b, bool norm) {
+  const int D = GBF_ODD, C = GBF_EVEN;
+  const size_t h = op->half();
+  const void* srcC = (const char*)src + C * h;
+  const void* srcD = (const char*)src + D * h;
+  void *s1 = op->T(8), *tC = op->T(9), *u = op->T(3);
+  op->local(s, C, srcC, tC, op->G());
+  op->dslash(s, D, false, tC, s1, op->none(), -1.0, srcD, 1.0);
+  op->dslash(s, C, true, s1, u, op->Gdag());
+  op->dslash(s, D, true, u, b, op->Gdag(), -1.0, s1, 1.0, op->none(), norm ? 2 : 0, nullptr, FIN_STORE);
+}
+
+// The solution from the odd-site solution y: x_D = A_D^-1 y,
+// x_C = A_C^-1 (src_C - Dhop G_D y)  (schur_complement_two.py:106-148)
+void eo2ne_reconstruct(gbf_op* op, cudaStream_t s, const void* src, const void* y, void* x) {
+  const int D = GBF_ODD, C = GBF_EVEN;
+  const size_t h = op->half();
+  const void* srcC = (const char*)src + C * h;
+  void* xC = (char*)x + C * h;
+  void* xD = (char*)x + D * h;
+  void *s1 = op->T(8), *tC = op->T(9);
+  op->local(s, D, y, xD, op->Ainv(false));
+  op->local(s, D, y, tC, op->G());
+  op->dslash(s, C, false, tC, s1, op->none(), -1.0, srcC, 1.0);
+  op->local(s, C, s1, xC, op->Ainv(false));
+}
+
+// The CG loop on the device state prepared in op->st (cp, rsq, done, p, r,
+// y = T(4), T(5), T(7)); returns whether the device loop ran and fills the
+// profile timings (cg.py:73-105)
+bool cg_loop(gbf_op* op, cudaStream_t s, const gbf_cg_params* prm, double* kms, int* kcount) {
+  if (prm->profile) {
+    // diagnostic: plain launches with CUDA events around each kernel class
+    cudaEvent_t ev[7];
+    for (int i = 0; i < 7; ++i) CK(cudaEventCreate(&ev[i]));
+    for (int it = 0; it < prm->maxiter; ++it) {
+      cg_iteration(op, s, ev);
+      CK(cudaEventSynchronize(ev[6]));
+      float ms;
+      CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      kms[1] += ms;
+      for (int i = 1; i < 5; ++i) {
+        CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+        kms[0] += ms;
+      }
+      CK(cudaEventElapsedTime(&ms, ev[5], ev[6]));
+      kms[2] += ms;
+      kcount[0] += 4;
+      kcount[1] += 1;
+      kcount[2] += 1;
+      CK(cudaMemcpy(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost));
+      if (op->hst->all_done) break;
+    }
+    for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+  }
+  bool device_loop = false;
+  if (!prm->profile && prm->iterations_per_graph <= 0) {
+    // ---- the whole CG loop on the device: a conditional while node whose
+    // body is one iteration; the CG update kernel sets the loop condition to
+    // !all_done (converged, maxiter reached or every rhs broken down), and
+    // its early exit sets it to 0, so the loop ends within maxiter + 1
+    // bodies.  No host round trip and no iteration past convergence. ----
+    device_loop = true;
+    if (!op->cgraph) {
+      cudaGraph_t gr;
+      CK(cudaGraphCreate(&gr, 0));
+      try {
+        cudaGraphConditionalHandle h;
+        CK(cudaGraphConditionalHandleCreate(&h, gr, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        CK(cudaGraphAddNode(&node, gr, nullptr, nullptr, 0, &np));
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        CK(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        op->cond = h;
+        op->cond_active = true;
+        try {
+          cg_iteration(op, s);
+        } catch (...) {
+          op->cond_active = false;
+          cudaGraph_t t;
+          cudaStreamEndCapture(s, &t);
+          throw;
+        }
+        op->cond_active = false;
+        cudaGraph_t t;
+        CK(cudaStreamEndCapture(s, &t));
+        CK(cudaGraphInstantiate(&op->cgraph, gr, 0));
+      } catch (...) {
+        cudaGraphDestroy(gr);
+        throw;
+      }
+      cudaGraphDestroy(gr);
+    }
+    CK(cudaGraphLaunch(op->cgraph, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  // ---- CG loop in graphs of K iterations, convergence checked by the host ----
+  const int K = prm->iterations_per_graph > 0 ? prm->iterations_per_graph : 8;
+  if (!prm->profile && !device_loop && (!op->graph || op->graph_K != K)) {
+    op->drop_graphs();
+    cudaGraph_t gr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int k = 0; k < K; ++k) cg_iteration(op, s);
+    } catch (...) {
+      cudaStreamEndCapture(s, &gr);
+      throw;
+    }
+    CK(cudaStreamEndCapture(s, &gr));
+    CK(cudaGraphInstantiate(&op->graph, gr, 0));
+    cudaGraphDestroy(gr);
+    op->graph_K = K;
+  }
+  const int max_launches = (prm->profile || device_loop) ? 0 : (prm->maxiter + K - 1) / K;
+  bool done = false;
+  int launched = 0;
+  for (; launched < max_launches && !done; ++launched) {
+    CK(cudaGraphLaunch(op->graph, s));
+    count_launch((unsigned long long)K * kKernelsPerIteration);
+    CK(cudaMemcpyAsync(op->hst + (launched & 1), op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(op->ev_chk[launched & 1], s));
+    if (launched > 0) {
+      CK(cudaEventSynchronize(op->ev_chk[(launched - 1) & 1]));
+      done = op->hst[(launched - 1) & 1].all_done != 0;
+    }
+  }
+  CK(cudaStreamSynchronize(s));
+  return device_loop;
+}
+
+// Results of a CG run from the final device state (synchronised)
+void cg_results(gbf_op* op, cudaStream_t s, cudaStream_t user, bool device_loop, const double* kms, const int* kcount,
+                gbf_cg_result* res) {
+  CK(cudaMemcpyAsync(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(op->ev_out, s));
+  CK(cudaStreamWaitEvent(user, op->ev_out, 0));
+  CK(cudaEventSynchronize(op->ev_out));
+  const CGState& st = op->hst[0];
+  if (device_loop) count_launch((unsigned long long)(st.iter > 0 ? st.iter : 1) * kKernelsPerIteration);
+  if (res) {
+    res->iterations = st.iter;
+    int conv = 1;
+    for (int k = 0; k < op->g.nrhs; ++k) {
+      const double b2 = st.last[k];  // |b|^2 of the system (FIN_STORE before the loop)
+      res->residual_sq[k] = b2 > 0 ? st.cp[k] / b2 : 0.0;
+      conv &= (st.cp[k] <= st.rsq[k]) ? 1 : 0;
+    }
+    res->converged = conv;
+    res->breakdown = st.breakdown;
+    for (int i = 0; i < 3; ++i) {
+      res->kernel_ms[i] = kms[i];
+      res->kernel_launches[i] = kcount[i];
+    }
+  }
+}
+
+void check_solve_args(gbf_op* op, const void* a, const void* b, const gbf_cg_params* prm) {
+  if (!op || !a || !b || !prm) throw Fail(GBF_E_ARG, "null argument");
+  if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+  ensure_ws(op);
+  for (int i = 0; i < 10; ++i) op->T(i);  // allocate before any graph capture
+}
+
+}  // namespace
+
+extern "C" {
+
 int gbf_solve_eo2ne_cg(gbf_op* op, const void* src, void* x, const gbf_cg_params* prm, gbf_cg_result* res, void* stream) {
   return guarded([&] {
-    if (!op || !src || !x || !prm) throw Fail(GBF_E_ARG, "null argument");
-    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
-    ensure_ws(op);
-    for (int i = 0; i < 10; ++i) op->T(i);  // allocate before any graph capture
+    check_solve_args(op, src, x, prm);
     cudaStream_t user = (cudaStream_t)stream;
     cudaStream_t s = op->stream;
     CK(cudaEventRecord(op->ev_in, user));
     CK(cudaStreamWaitEvent(s, op->ev_in, 0));
-    const int D = GBF_ODD, C = GBF_EVEN;
     const size_t h = op->half();
-    const void* srcC = (const char*)src + C * h;
-    const void* srcD = (const char*)src + D * h;
-    void* xC = (char*)x + C * h;
-    void* xD = (char*)x + D * h;
-    void *p = op->T(4), *r = op->T(5), *y = op->T(7), *s1 = op->T(8), *tC = op->T(9), *u = op->T(3);
-    // ---- prepare: r = Mpc^+ (src_D - Dhop G_C src_C)  (R_ne, normal_equation.py:47-48) ----
-    op->local(s, C, srcC, tC, op->G());
-    op->dslash(s, D, false, tC, s1, op->none(), -1.0, srcD, 1.0);
-    op->dslash(s, C, true, s1, u, op->Gdag());
-    op->dslash(s, D, true, u, r, op->Gdag(), -1.0, s1, 1.0, op->none(), 2, nullptr, FIN_STORE);
+    void *p = op->T(4), *r = op->T(5), *y = op->T(7);
+    // ---- prepare: r = R_ne src, |r|^2 -> state; CG from y = 0 ----
+    eo2ne_prepare(op, s, src, r, true);
     CK(launch_cg_init(op->st, op->g.nrhs, prm->eps, prm->maxiter, s));
     count_launch();
     CK(cudaMemsetAsync(p, 0, h, s));
     CK(cudaMemsetAsync(y, 0, h, s));
     double kms[3] = {0, 0, 0};
     int kcount[3] = {0, 0, 0};
-    if (prm->profile) {
-      // diagnostic: plain launches with CUDA events around each kernel class
-      cudaEvent_t ev[7];
-      for (int i = 0; i < 7; ++i) CK(cudaEventCreate(&ev[i]));
-      for (int it = 0; it < prm->maxiter; ++it) {
-        cg_iteration(op, s, ev);
-        CK(cudaEventSynchronize(ev[6]));
-        float ms;
-        CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-        kms[1] += ms;
-        for (int i = 1; i < 5; ++i) {
-          CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
-          kms[0] += ms;
-        }
-        CK(cudaEventElapsedTime(&ms, ev[5], ev[6]));
-        kms[2] += ms;
-        kcount[0] += 4;
-        kcount[1] += 1;
-        kcount[2] += 1;
-        CK(cudaMemcpy(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost));
-        if (op->hst->all_done) break;
-      }
-      for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
-    }
-    bool device_loop = false;
-    if (!prm->profile && prm->iterations_per_graph <= 0) {
-      // ---- the whole CG loop on the device: a conditional while node whose
-      // body is one iteration; the CG update kernel sets the loop condition to
-      // !all_done (converged, maxiter reached or every rhs broken down), and
-      // its early exit sets it to 0, so the loop ends within maxiter + 1
-      // bodies.  No host round trip and no iteration past convergence. ----
-      device_loop = true;
-      if (!op->cgraph) {
-        cudaGraph_t gr;
-        CK(cudaGraphCreate(&gr, 0));
-        try {
-          cudaGraphConditionalHandle h;
-          CK(cudaGraphConditionalHandleCreate(&h, gr, 1, cudaGraphCondAssignDefault));
-          cudaGraphNodeParams np{};
-          np.type = cudaGraphNodeTypeConditional;
-          np.conditional.handle = h;
-          np.conditional.type = cudaGraphCondTypeWhile;
-          np.conditional.size = 1;
-          cudaGraphNode_t node;
-          CK(cudaGraphAddNode(&node, gr, nullptr, nullptr, 0, &np));
-          cudaGraph_t body = np.conditional.phGraph_out[0];
-          CK(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-          op->cond = h;
-          op->cond_active = true;
-          try {
-            cg_iteration(op, s);
-          } catch (...) {
-            op->cond_active = false;
-            cudaGraph_t t;
-            cudaStreamEndCapture(s, &t);
-            throw;
-          }
-          op->cond_active = false;
-          cudaGraph_t t;
-          CK(cudaStreamEndCapture(s, &t));
-          CK(cudaGraphInstantiate(&op->cgraph, gr, 0));
-        } catch (...) {
-          cudaGraphDestroy(gr);
-          throw;
-        }
-        cudaGraphDestroy(gr);
-      }
-      CK(cudaGraphLaunch(op->cgraph, s));
-      CK(cudaStreamSynchronize(s));
-    }
-    // ---- CG loop in graphs of K iterations, convergence checked by the host ----
-    const int K = prm->iterations_per_graph > 0 ? prm->iterations_per_graph : 8;
-    if (!prm->profile && !device_loop && (!op->graph || op->graph_K != K)) {
-      op->drop_graphs();
-      cudaGraph_t gr;
-      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      try {
-        for (int k = 0; k < K; ++k) cg_iteration(op, s);
-      } catch (...) {
-        cudaStreamEndCapture(s, &gr);
-        throw;
-      }
-      CK(cudaStreamEndCapture(s, &gr));
-      CK(cudaGraphInstantiate(&op->graph, gr, 0));
-      cudaGraphDestroy(gr);
-      op->graph_K = K;
-    }
-    const int max_launches = (prm->profile || device_loop) ? 0 : (prm->maxiter + K - 1) / K;
-    bool done = false;
-    int launched = 0;
-    for (; launched < max_launches && !done; ++launched) {
-      CK(cudaGraphLaunch(op->graph, s));
-      count_launch((unsigned long long)K * kKernelsPerIteration);
-      CK(cudaMemcpyAsync(op->hst + (launched & 1), op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
-      CK(cudaEventRecord(op->ev_chk[launched & 1], s));
-      if (launched > 0) {
-        CK(cudaEventSynchronize(op->ev_chk[(launched - 1) & 1]));
-        done = op->hst[(launched - 1) & 1].all_done != 0;
-      }
-    }
-    CK(cudaStreamSynchronize(s));
+    const bool device_loop = cg_loop(op, s, prm, kms, kcount);
     // ---- reconstruct: x_D = A^-1 y ; x_C = A_C^-1 (src_C - Dhop G y) ----
-    op->local(s, D, y, xD, op->Ainv(false));
-    op->local(s, D, y, tC, op->G());
-    op->dslash(s, C, false, tC, s1, op->none(), -1.0, srcC, 1.0);
-    op->local(s, C, s1, xC, op->Ainv(false));
-    CK(cudaMemcpyAsync(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(op->ev_out, s));
-    CK(cudaStreamWaitEvent(user, op->ev_out, 0));
-    CK(cudaEventSynchronize(op->ev_out));
-    const CGState& st = op->hst[0];
-    if (device_loop) count_launch((unsigned long long)(st.iter > 0 ? st.iter : 1) * kKernelsPerIteration);
-    if (res) {
-      res->iterations = st.iter;
-      int conv = 1;
-      for (int k = 0; k < op->g.nrhs; ++k) {
-        const double b2 = st.last[k];  // |b|^2 of the eo2_ne system from the prepare reduction
-        res->residual_sq[k] = b2 > 0 ? st.cp[k] / b2 : 0.0;
-        conv &= (st.cp[k] <= st.rsq[k]) ? 1 : 0;
+    eo2ne_reconstruct(op, s, src, y, x);
+    cg_results(op, s, user, device_loop, kms, kcount, res);
+  });
+}
+
+int gbf_solve_normal_cg(gbf_op* op, const void* b, void* x, const gbf_cg_params* prm, gbf_cg_result* res, void* stream) {
+  return guarded([&] {
+    check_solve_args(op, b, x, prm);
+    if (b == x) throw Fail(GBF_E_ARG, "source and solution must differ");
+    cudaStream_t user = (cudaStream_t)stream;
+    cudaStream_t s = op->stream;
+    CK(cudaEventRecord(op->ev_in, user));
+    CK(cudaStreamWaitEvent(s, op->ev_in, 0));
+    const size_t h = op->half();
+    void *p = op->T(4), *r = op->T(5), *mmp = op->T(6), *y = op->T(7);
+    const int nr = op->g.nrhs;
+    // |b|^2 -> state (FIN_STORE), then rsq = eps^2 |b|^2
+    BlasArgs nb{};
+    nb.g = op->g;
+    nb.x = b;
+    nb.y = b;
+    nb.red = 3;
+    nb.ra = op->red(FIN_STORE);
+    CK(launch_blas(op->prec, nb, s));
+    count_launch();
+    double b2[kMaxRhs];
+    read_last(op, s, b2, nullptr);
+    bool zero = true;
+    for (int k = 0; k < nr; ++k) zero = zero && b2[k] == 0.0;
+    if (zero) {
+      // cg.py:66-68: a zero source has the zero solution
+      CK(cudaMemsetAsync(x, 0, h, s));
+      CK(cudaEventRecord(op->ev_out, s));
+      CK(cudaStreamWaitEvent(user, op->ev_out, 0));
+      CK(cudaStreamSynchronize(s));
+      if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->converged = 1;
       }
-      res->converged = conv;
-      res->breakdown = st.breakdown;
-      for (int i = 0; i < 3; ++i) {
-        res->kernel_ms[i] = kms[i];
-        res->kernel_launches[i] = kcount[i];
+      return;
+    }
+    CK(launch_cg_init(op->st, nr, prm->eps, prm->maxiter, s));
+    count_launch();
+    // r = b - A x (the guess), |r|^2 -> cp and the done flags (FIN_INIT)
+    apply_ne(op, s, x, mmp);
+    BlasArgs ra{};
+    ra.g = op->g;
+    ra.out = r;
+    ra.x = mmp;
+    ra.y = b;
+    for (int k = 0; k < nr; ++k) {
+      ra.a_re[k] = -1.0;
+      ra.b_re[k] = 1.0;
+    }
+    ra.write = 1;
+    ra.red = 2;
+    ra.ra = op->red(FIN_INIT);
+    CK(launch_blas(op->prec, ra, s));
+    count_launch();
+    CK(cudaMemcpyAsync(y, x, h, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(p, 0, h, s));
+    double kms[3] = {0, 0, 0};
+    int kcount[3] = {0, 0, 0};
+    const bool device_loop = cg_loop(op, s, prm, kms, kcount);
+    CK(cudaMemcpyAsync(x, y, h, cudaMemcpyDeviceToDevice, s));
+    cg_results(op, s, user, device_loop, kms, kcount, res);
+  });
+}
+
+int gbf_eo2ne_prepare(gbf_op* op, const void* src, void* b, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !b) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    ensure_ws(op);
+    eo2ne_prepare(op, (cudaStream_t)stream, src, b, false);
+  });
+}
+
+int gbf_eo2ne_reconstruct(gbf_op* op, const void* src, const void* y, void* x, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !y || !x) throw Fail(GBF_E_ARG, "null argument");
+    if (!op->gauge_set) throw Fail(GBF_E_ARG, "gauge field not set (gbf_update_gauge)");
+    if (x == src || x == y) throw Fail(GBF_E_ARG, "the solution must not alias the inputs");
+    ensure_ws(op);
+    eo2ne_reconstruct(op, (cudaStream_t)stream, src, y, x);
+  });
+}
+
+// dst = sum_n left_n <right_n, src> f_n  (lib/gpt/algorithms/modes/matrix.py:31-56)
+int gbf_modes_apply(gbf_op* op, const void* const* left, const void* const* right, const double* f, int n,
+                    const void* src, void* dst, int nhalves, void* stream) {
+  return guarded([&] {
+    if (!op || !left || !right || !f || !src || !dst) throw Fail(GBF_E_ARG, "null argument");
+    if (n < 1) throw Fail(GBF_E_ARG, "at least one mode");
+    if (nhalves != 1 && nhalves != 2) throw Fail(GBF_E_ARG, "nhalves must be 1 or 2");
+    if (src == dst) throw Fail(GBF_E_ARG, "src and dst must differ (as in the reference)");
+    if (op->g.nrhs != 1) throw Fail(GBF_E_UNSUPPORTED, "mode representations act on fields with one right-hand side");
+    for (int i = 0; i < n; ++i) {
+      if (!left[i] || !right[i]) throw Fail(GBF_E_ARG, "null mode");
+      if (left[i] == dst) throw Fail(GBF_E_ARG, "dst must not be a mode");
+    }
+    ensure_ws(op);
+    if (!op->mode_dev) op->mode_dev = (double2*)dmalloc(kModeBlock * sizeof(double2));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t h = op->half();
+    // w_n = f_n <right_n, src>, summed over the halves
+    std::vector<std::complex<double>> w(n, 0.0);
+    for (int i0 = 0; i0 < n; i0 += kModeBlock) {
+      const int m = std::min(kModeBlock, n - i0);
+      for (int hf = 0; hf < nhalves; ++hf) {
+        ModeDotArgs a{};
+        for (int j = 0; j < m; ++j) a.v[j] = (const char*)right[i0 + j] + hf * h;
+        a.n = m;
+        a.src = (const char*)src + hf * h;
+        a.partial = op->partial;
+        a.counter = op->counter;
+        a.out = op->mode_dev;
+        CK(launch_mode_dot(op->prec, op->g, a, op->partial_cap, s));
+        count_launch();
+        double2 c[kModeBlock];
+        CK(cudaMemcpyAsync(c, op->mode_dev, m * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int j = 0; j < m; ++j) w[i0 + j] += std::complex<double>(c[j].x, c[j].y);
+      }
+    }
+    for (int i = 0; i < n; ++i) w[i] *= std::complex<double>(f[2 * i], f[2 * i + 1]);
+    // dst = sum_n w_n left_n, kModeBlock modes per pass
+    for (int hf = 0; hf < nhalves; ++hf) {
+      for (int i0 = 0; i0 < n; i0 += kModeBlock) {
+        const int m = std::min(kModeBlock, n - i0);
+        ModeAxpyArgs a{};
+        for (int j = 0; j < m; ++j) {
+          a.v[j] = (const char*)left[i0 + j] + hf * h;
+          a.w[j] = make_double2(w[i0 + j].real(), w[i0 + j].imag());
+        }
+        a.n = m;
+        a.out = (char*)dst + hf * h;
+        a.accumulate = i0 > 0;
+        CK(launch_mode_axpy(op->prec, op->g, a, s));
+        count_launch();
       }
     }
   });

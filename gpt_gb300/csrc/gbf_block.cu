@@ -368,3 +368,140 @@ cudaError_t launch_multishift(int P, const Geo& g, const MultiShiftArgs& a, cuda
 }
 
 }  // namespace gbf
+
+namespace gbf {
+
+// ---------------------------------------------------------------------------
+// Mode representation A = sum_n left_n right_n^+ f(eval_n)
+// (lib/gpt/algorithms/modes/matrix.py:31-56: rank_inner_product of a block of
+// the right modes with the source, then the linear combination of the left
+// modes), used by the deflation inverter (lib/gpt/algorithms/inverter/
+// deflate.py).  Every mode is a separate field; both kernels stream a block
+// of up to kModeBlock of them through one pass over the sites.
+// ---------------------------------------------------------------------------
+
+// out[j] = sum_sites conj(v_j) . src: per-site products in the arithmetic
+// precision summed per thread in FP64, FP64 block sums in a fixed order, the
+// last block sums the [block][j] partials in block order (deterministic).
+// bytes/site: src once + every v_j once.
+template <int P>
+__global__ void __launch_bounds__(256) mode_dot_kernel(const Geo g, const ModeDotArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  __shared__ double sm[64];
+  const int t = threadIdx.x;
+  double re[kModeBlock], im[kModeBlock];
+#pragma unroll
+  for (int j = 0; j < kModeBlock; ++j) re[j] = im[j] = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long n = (long long)blockIdx.x * blockDim.x + t; n < g.N; n += stride) {
+    V s[12];
+    load_spinor<P>(a.src, g.N, n, s);
+#pragma unroll
+    for (int j = 0; j < kModeBlock; ++j) {
+      if (j < a.n) {
+        V v[12];
+        load_spinor<P>(a.v[j], g.N, n, v);
+        double dr, di;
+        site_dot<R>(v, s, dr, di);
+        re[j] += dr;
+        im[j] += di;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kModeBlock; ++j) {
+    if (j < a.n) {
+      const double2 b = block_sum_shfl(re[j], im[j], sm);
+      if (t == 0) a.partial[(size_t)blockIdx.x * a.n + j] = b;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ int s_last;
+  if (t == 0) s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (t < a.n) {
+    double sr = 0.0, si = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+      const double2 v = __ldcg(a.partial + (size_t)b * a.n + t);
+      sr += v.x;
+      si += v.y;
+    }
+    a.out[t] = make_double2(sr, si);
+  }
+  if (t == 0) *a.counter = 0u;
+}
+
+// out = (accumulate ? out : 0) + sum_j w_j v_j, complex weights rounded to
+// the arithmetic precision.  bytes/site: every v_j once, out written (+ read).
+template <int P>
+__global__ void __launch_bounds__(256) mode_axpy_kernel(const Geo g, const ModeAxpyArgs a) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
+    V o[12];
+    if (a.accumulate) {
+      load_spinor<P>(a.out, g.N, n, o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) o[k] = cz<R>();
+    }
+#pragma unroll 1
+    for (int j = 0; j < a.n; ++j) {
+      V v[12];
+      load_spinor<P>(a.v[j], g.N, n, v);
+      const V w = mk<R>((R)a.w[j].x, (R)a.w[j].y);
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        nrm<R>(v[k]);
+        o[k] = cmadd<R>(o[k], w, v[k]);
+        nrm<R>(o[k]);
+      }
+    }
+    store_spinor<P>(a.out, g.N, n, o);
+  }
+}
+
+template <int P>
+static cudaError_t launch_mode_dot_t(const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st) {
+  auto k = mode_dot_kernel<P>;
+  const int bd = 256;
+  long long nb = reduce_grid((g.N + bd - 1) / bd, 1, resident_blocks((const void*)k, bd, 0));
+  if (nb * a.n > max_partials) nb = max_partials / a.n;
+  if (nb < 1) return cudaErrorInvalidValue;
+  k<<<(unsigned)nb, bd, 0, st>>>(g, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mode_dot(int P, const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st) {
+  if (a.n < 1 || a.n > kModeBlock) return cudaErrorInvalidValue;
+  if (P == P64) return launch_mode_dot_t<P64>(g, a, max_partials, st);
+  if (P == P32) return launch_mode_dot_t<P32>(g, a, max_partials, st);
+  if (P == P16) return launch_mode_dot_t<P16>(g, a, max_partials, st);
+  if (P == PDD) return launch_mode_dot_t<PDD>(g, a, max_partials, st);
+  return cudaErrorInvalidValue;
+}
+
+template <int P>
+static cudaError_t launch_mode_axpy_t(const Geo& g, const ModeAxpyArgs& a, cudaStream_t st) {
+  auto k = mode_axpy_kernel<P>;
+  const int bd = 256;
+  const long long nb = reduce_grid((g.N + bd - 1) / bd, 1, resident_blocks((const void*)k, bd, 0));
+  k<<<(unsigned)nb, bd, 0, st>>>(g, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mode_axpy(int P, const Geo& g, const ModeAxpyArgs& a, cudaStream_t st) {
+  if (a.n < 0 || a.n > kModeBlock) return cudaErrorInvalidValue;
+  if (P == P64) return launch_mode_axpy_t<P64>(g, a, st);
+  if (P == P32) return launch_mode_axpy_t<P32>(g, a, st);
+  if (P == P16) return launch_mode_axpy_t<P16>(g, a, st);
+  if (P == PDD) return launch_mode_axpy_t<PDD>(g, a, st);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gbf

@@ -125,4 +125,25 @@ cudaError_t launch_lincomb2(int P, const Geo& g, void* out1, const void* Y1, dou
                             void* out2, const void* Y2, double b2, double c, const void* X2, const double2* W2,
                             cudaStream_t st);
 
+// mode representation (gbf_block.cu): inner products of a block of separate
+// fields with one field, and their linear combination
+constexpr int kModeBlock = 8;
+struct ModeDotArgs {
+  const void* v[kModeBlock];
+  int n;
+  const void* src;
+  double2* partial;   // [gridDim][n]
+  unsigned* counter;  // zero on entry, restored
+  double2* out;       // out[j] = sum conj(v_j) . src
+};
+struct ModeAxpyArgs {
+  const void* v[kModeBlock];
+  double2 w[kModeBlock];
+  int n;
+  void* out;       // out = (accumulate ? out : 0) + sum_j w_j v_j
+  int accumulate;
+};
+cudaError_t launch_mode_dot(int P, const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st);
+cudaError_t launch_mode_axpy(int P, const Geo& g, const ModeAxpyArgs& a, cudaStream_t st);
+
 }  // namespace gbf

@@ -177,6 +177,38 @@ int gbf_apply_eo2ne_normal(gbf_op* op, const void* in, void* out, void* stream);
 int gbf_solve_eo2ne_multishift(gbf_op* op, const void* src, void* const* x, const double* shifts, int n,
                                const gbf_cg_params* p, gbf_cg_result* res, void* stream);
 
+/* cg(eps, maxiter) applied to the eo2_ne normal operator itself
+ * (lib/gpt/algorithms/inverter/cg.py:47-105 with the guess the reference
+ * takes from dst, :48-68): solves Mpc^+ Mpc x = b on odd-site half fields,
+ * starting from x as passed in (zero allowed) and overwriting it with the
+ * solution; b = 0 gives x = 0.  Converged when |r|^2 <= eps^2 |b|^2 (checked
+ * before the first iteration too); residual_sq = |r|^2 / |b|^2.  The loop
+ * is the one of gbf_solve_eo2ne_cg (device loop, iterations_per_graph,
+ * profile).  This is the inner solve of inverter.sequence(deflate(...), cg)
+ * (lib/gpt/algorithms/inverter/sequence.py:23-42). */
+int gbf_solve_normal_cg(gbf_op* op, const void* b, void* x, const gbf_cg_params* p, gbf_cg_result* res, void* stream);
+
+/* The two halves of preconditioned(eo2_ne(), inverter) around an arbitrary
+ * inverter of the normal operator (lib/gpt/algorithms/inverter/
+ * preconditioned.py:36-44): prepare writes the odd-site right-hand side
+ * b = Mpc^+ (src_D - Dhop G_C src_C) of the full field src
+ * (normal_equation.py:47-48, schur_complement_two.py:87-104); reconstruct
+ * writes the full solution x from the odd-site solution y
+ * (schur_complement_two.py:106-148). */
+int gbf_eo2ne_prepare(gbf_op* op, const void* src, void* b, void* stream);
+int gbf_eo2ne_reconstruct(gbf_op* op, const void* src, const void* y, void* x, void* stream);
+
+/* Mode representation dst = sum_n left[n] <right[n], src> f[n]
+ * (lib/gpt/algorithms/modes/matrix.py:31-56; the deflation inverter
+ * lib/gpt/algorithms/inverter/deflate.py is left = right = eigenvectors,
+ * f = 1 / eigenvalue).  left/right: n device fields of op's layout with
+ * nhalves halves (1: one checkerboard, 2: full), n_rhs = 1; f: n complex
+ * numbers as 2n doubles (re, im).  Inner products are reduced
+ * deterministically in FP64 (blocks of 8 modes per pass over the sites);
+ * src must differ from dst, and dst from every left mode. */
+int gbf_modes_apply(gbf_op* op, const void* const* left, const void* const* right, const double* f, int n,
+                    const void* src, void* dst, int nhalves, void* stream);
+
 /* Autotuner (the role of lib/gpt/core/auto_tune.py for this library): times
  * the block-size candidates of the four kernel classes -- [0] hopping kernel
  * with a per-thread epilogue, [1] hopping kernel with the Mobius s-matrix
