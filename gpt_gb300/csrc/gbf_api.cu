@@ -1250,6 +1250,43 @@ int gbf_solve_normal_cg(gbf_op* op, const void* b, void* x, const gbf_cg_params*
   });
 }
 
+// MADWF fifth-dimension moves (lib/gpt/qcd/fermion/preconditioner/mixed_dwf.py:43-98)
+int gbf_chiral_shift(gbf_op* op, const void* src, void* dst, int offset, int nhalves, void* stream) {
+  return guarded([&] {
+    if (!op || !src || !dst) throw Fail(GBF_E_ARG, "null argument");
+    if (nhalves != 1 && nhalves != 2) throw Fail(GBF_E_ARG, "nhalves must be 1 or 2");
+    if (src == dst) throw Fail(GBF_E_ARG, "src and dst must differ");
+    const size_t h = op->half();
+    for (int hf = 0; hf < nhalves; ++hf) {
+      CK(launch_chiral_shift(op->prec, op->g, (const char*)src + hf * h, (char*)dst + hf * h, offset,
+                             (cudaStream_t)stream));
+      count_launch();
+    }
+  });
+}
+
+int gbf_copy_slices(gbf_op* dst_op, void* dst, int dst_s0, gbf_op* src_op, const void* src, int src_s0, int count,
+                    double scale, int nhalves, void* stream) {
+  return guarded([&] {
+    if (!dst_op || !src_op || !dst || !src) throw Fail(GBF_E_ARG, "null argument");
+    if (nhalves != 1 && nhalves != 2) throw Fail(GBF_E_ARG, "nhalves must be 1 or 2");
+    const Geo &gd = dst_op->g, &gs = src_op->g;
+    if (dst_op->prec != src_op->prec) throw Fail(GBF_E_ARG, "fields of different precision");
+    for (int m = 0; m < 4; ++m)
+      if (gd.L[m] != gs.L[m]) throw Fail(GBF_E_ARG, "fields of different 4D geometry");
+    if (gd.nrhs != gs.nrhs) throw Fail(GBF_E_ARG, "fields with different n_rhs");
+    if (count < 0 || dst_s0 < 0 || src_s0 < 0 || dst_s0 + count > gd.Ls || src_s0 + count > gs.Ls)
+      throw Fail(GBF_E_ARG, "slice range outside the fifth dimension");
+    if (src == dst && dst_s0 != src_s0) throw Fail(GBF_E_ARG, "overlapping slice copy");
+    const size_t hd = dst_op->half(), hs = src_op->half();
+    for (int hf = 0; hf < nhalves; ++hf) {
+      CK(launch_copy_slices(dst_op->prec, gd, (char*)dst + hf * hd, dst_s0, gs, (const char*)src + hf * hs, src_s0,
+                            count, scale, (cudaStream_t)stream));
+      count_launch();
+    }
+  });
+}
+
 int gbf_eo2ne_prepare(gbf_op* op, const void* src, void* b, void* stream) {
   return guarded([&] {
     if (!op || !src || !b) throw Fail(GBF_E_ARG, "null argument");

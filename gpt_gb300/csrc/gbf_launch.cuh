@@ -146,4 +146,11 @@ struct ModeAxpyArgs {
 cudaError_t launch_mode_dot(int P, const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st);
 cudaError_t launch_mode_axpy(int P, const Geo& g, const ModeAxpyArgs& a, cudaStream_t st);
 
+// fifth-dimension moves of the MADWF preconditioner (gbf_local.cu):
+// dst_s = P- src_s + P+ src_{s + offset}, and a slice copy between fields of
+// possibly different Ls (same 4D geometry and nrhs, one half)
+cudaError_t launch_chiral_shift(int P, const Geo& g, const void* src, void* dst, int offset, cudaStream_t st);
+cudaError_t launch_copy_slices(int P, const Geo& gd, void* dst, int d0, const Geo& gs, const void* src, int s0, int count,
+                               double scale, cudaStream_t st);
+
 }  // namespace gbf

@@ -679,3 +679,94 @@ cudaError_t launch_split_dd(const void* src64, void* dst, long long n_complex, c
 }
 
 }  // namespace gbf
+
+namespace gbf {
+
+// ---------------------------------------------------------------------------
+// Fifth-dimension data movement of the MADWF preconditioner
+// (lib/gpt/qcd/fermion/preconditioner/mixed_dwf.py:43-98).  Thread per 5D
+// site; bytes/site: two reads and one write (chiral shift), one read and one
+// write (slice copy).
+// ---------------------------------------------------------------------------
+
+// dst_s = P- src_s + P+ src_{(s + offset) mod Ls}, P+- = (1 +- gamma5) / 2 with
+// gamma5 = diag(1, 1, -1, -1): spins 0, 1 from slice s + offset, spins 2, 3
+// from slice s (the operator P of mixed_dwf.py:46-54; offset -1 is P^+ = P^-1)
+template <int P>
+__global__ void __launch_bounds__(256) chiral_shift_kernel(const Geo g, const void* src, void* dst, int offset) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  const unsigned cb = g.fN5.div((unsigned)n);
+  const unsigned i5 = (unsigned)n - cb * (unsigned)g.N5;
+  const unsigned rhs = g.fLs.div(i5);
+  const int s = (int)(i5 - rhs * (unsigned)g.Ls);
+  int s2 = (s + offset) % g.Ls;
+  if (s2 < 0) s2 += g.Ls;
+  const long long n2 = (long long)cb * g.N5 + (long long)rhs * g.Ls + s2;
+  V a[12], b[12];
+  load_spinor<P>(src, g.N, n, a);
+  load_spinor<P>(src, g.N, n2, b);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a[k] = b[k];
+  store_spinor<P>(dst, g.N, n, a);
+}
+
+// dst slices [d0, d0 + count) = scale * src slices [s0, s0 + count), every
+// 4D site and right-hand side; the two fields may have different Ls
+// (g.separate / g.merge along the fifth dimension, mixed_dwf.py:43-48)
+template <int P>
+__global__ void __launch_bounds__(256) copy_slices_kernel(const Geo gd, void* dst, int d0, const Geo gs, const void* src,
+                                                          int s0, int count, double scale) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)gs.Vh * gs.nrhs * count;
+  if (t >= total) return;
+  const long long q = t / count;
+  const int j = (int)(t - q * count);
+  const long long cb = q / gs.nrhs;
+  const int rhs = (int)(q - cb * gs.nrhs);
+  const long long ns = cb * gs.N5 + (long long)rhs * gs.Ls + s0 + j;
+  const long long nd = cb * gd.N5 + (long long)rhs * gd.Ls + d0 + j;
+  V v[12];
+  load_spinor<P>(src, gs.N, ns, v);
+  if (scale != 1.0) {
+    const R sc = (R)scale;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      nrm<R>(v[k]);
+      v[k] = scl<R>(sc, v[k]);
+      nrm<R>(v[k]);
+    }
+  }
+  store_spinor<P>(dst, gd.N, nd, v);
+}
+
+cudaError_t launch_chiral_shift(int P, const Geo& g, const void* src, void* dst, int offset, cudaStream_t st) {
+  const int bd = 256;
+  const unsigned nb = (unsigned)((g.N + bd - 1) / bd);
+  if (P == P64) chiral_shift_kernel<P64><<<nb, bd, 0, st>>>(g, src, dst, offset);
+  else if (P == P32) chiral_shift_kernel<P32><<<nb, bd, 0, st>>>(g, src, dst, offset);
+  else if (P == P16) chiral_shift_kernel<P16><<<nb, bd, 0, st>>>(g, src, dst, offset);
+  else if (P == PDD) chiral_shift_kernel<PDD><<<nb, bd, 0, st>>>(g, src, dst, offset);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_slices(int P, const Geo& gd, void* dst, int d0, const Geo& gs, const void* src, int s0, int count,
+                               double scale, cudaStream_t st) {
+  const int bd = 256;
+  const long long total = (long long)gs.Vh * gs.nrhs * count;
+  if (total == 0) return cudaSuccess;
+  const unsigned nb = (unsigned)((total + bd - 1) / bd);
+  if (P == P64) copy_slices_kernel<P64><<<nb, bd, 0, st>>>(gd, dst, d0, gs, src, s0, count, scale);
+  else if (P == P32) copy_slices_kernel<P32><<<nb, bd, 0, st>>>(gd, dst, d0, gs, src, s0, count, scale);
+  else if (P == P16) copy_slices_kernel<P16><<<nb, bd, 0, st>>>(gd, dst, d0, gs, src, s0, count, scale);
+  else if (P == PDD) copy_slices_kernel<PDD><<<nb, bd, 0, st>>>(gd, dst, d0, gs, src, s0, count, scale);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace gbf

@@ -176,6 +176,18 @@ class fermion_operator(matrix_operator):
     def updated(self, U):
         return type(self)(U, self.params, precision=self.precision, daggered=self.daggered)
 
+    def modified(self, **params):
+        """The same operator with some parameters replaced (base.py:221-228),
+        for example modified(mass=1.0) for the Pauli-Villars operator of
+        MADWF; mass sets both Mobius masses, as the factories do."""
+        p = {**self.params, **params}
+        if "mass" in params and self.name in ("mobius", "zmobius"):
+            p["mass_plus"] = p["mass_minus"] = float(params["mass"])
+        if "kappa" in params and self.name in ("wilson_clover", "wilson_twisted_mass"):
+            p["mass"] = 1.0 / float(params["kappa"]) / 2.0 - 4.0
+            p.pop("kappa")
+        return type(self)(self.U, p, precision=self.precision, daggered=self.daggered)
+
     def adj(self):
         return type(self)(self.U, self.params, precision=self.precision, daggered=not self.daggered)
 
@@ -336,6 +348,77 @@ class preconditioner:
 
         def __call__(self, op):
             return _eo2_ne_matrix(op, self.parity)
+
+    class mixed_dwf:
+        """MADWF (lib/gpt/qcd/fermion/preconditioner/mixed_dwf.py:29-108, the
+        algorithm of arXiv:1111.5059): an approximate inverse of the outer
+        domain-wall operator from a solve with a cheaper inner one (another
+        Ls or zmobius), through the Pauli-Villars operators (mass 1) and the
+        chiral shift P.  solver and solver_pv are inverters of full 5D
+        operators (for example preconditioned(eo2_ne(), cg(...))); all
+        fifth-dimension moves run on the device (gbf_chiral_shift,
+        gbf_copy_slices).  Inner and outer operators share the precision."""
+
+        def __init__(self, solver, solver_pv, dwf_inner):
+            self.solver = solver
+            self.solver_pv = solver_pv
+            self.dwf_inner = dwf_inner
+            self.dwf_inner_pv = dwf_inner.modified(mass=1.0)
+
+        def __call__(self, dwf_outer):
+            inner, inner_pv = self.dwf_inner, self.dwf_inner_pv
+            if inner.precision is not dwf_outer.precision:
+                raise ValueError("inner and outer domain-wall operators must share the precision")
+            if inner.n_rhs != dwf_outer.n_rhs or inner.U_grid.fdimensions != dwf_outer.U_grid.fdimensions:
+                raise ValueError("inner and outer domain-wall operators must share the 4D grid and n_rhs")
+            outer_pv = dwf_outer.modified(mass=1.0)
+            inv_outer_pv = self.solver_pv(outer_pv)
+            inv_inner = self.solver(inner)
+            L = _lib.load()
+
+            def P(dst, src, offset):
+                # offset 1: P (mixed_dwf.py:56-57); offset -1: P^+ = P^-1 (:59-60)
+                _lib.check(L.gbf_chiral_shift(src.layout.op, src.ptr, dst.ptr, offset, src.nhalves(), core.stream_ptr()))
+
+            def slice0(dst, src, scale):
+                _lib.check(L.gbf_copy_slices(dst.layout.op, dst.ptr, 0, src.layout.op, src.ptr, 0, 1, float(scale),
+                                             src.nhalves(), core.stream_ptr()))
+
+            def one(dst, src):
+                # c_s = P^+ D_PV,outer^-1 src
+                c = dwf_outer.F_lattice()
+                P(c, inv_outer_pv(src), -1)
+                # y0' = [P^+ D_inner^-1 D_PV,inner P (c_0, 0, ..., 0)]_0 on the inner Ls
+                wi = inner.F_lattice()
+                slice0(wi, c, 1.0)
+                a = inner.F_lattice()
+                P(a, wi, 1)
+                y = inv_inner(inner_pv.M(a))
+                y0 = inner.F_lattice()
+                P(y0, y, -1)
+                # y1 = P^+ D_PV,outer^-1 D_outer P (-y0', c_1, ..., c_{Ls-1})
+                wo = c.copy()
+                slice0(wo, y0, -1.0)
+                e = dwf_outer.F_lattice()
+                P(e, wo, 1)
+                y1 = dwf_outer.F_lattice()
+                P(y1, inv_outer_pv(dwf_outer.M(e)), -1)
+                # dst = P (y0', y1_1, ..., y1_{Ls-1})
+                slice0(y1, y0, 1.0)
+                P(dst, y1, 1)
+                dst.cb = core.full
+
+            def inv(dst, src):
+                if isinstance(src, (list, tuple)):
+                    for d, s_ in zip(dst, src):
+                        one(d, s_)
+                else:
+                    one(dst, src)
+
+            m = matrix_operator(inv, inv_mat=dwf_outer.mat)
+            m._new_dst = lambda src: ([dwf_outer.F_lattice() for _ in src] if isinstance(src, (list, tuple))
+                                      else dwf_outer.F_lattice())
+            return m
 
 
 class _eo2_ne_matrix:

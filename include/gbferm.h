@@ -198,6 +198,19 @@ int gbf_solve_normal_cg(gbf_op* op, const void* b, void* x, const gbf_cg_params*
 int gbf_eo2ne_prepare(gbf_op* op, const void* src, void* b, void* stream);
 int gbf_eo2ne_reconstruct(gbf_op* op, const void* src, const void* y, void* x, void* stream);
 
+/* The fifth-dimension moves of the MADWF preconditioner
+ * (lib/gpt/qcd/fermion/preconditioner/mixed_dwf.py:43-98) on fields of a
+ * mobius/zmobius layout.  gbf_chiral_shift: dst_s = P- src_s + P+ src_{s+offset}
+ * (s + offset mod Ls, P+- = (1 +- gamma5)/2), the operator P of mixed_dwf.py
+ * for offset = 1 and its inverse P^+ for offset = -1; src != dst.
+ * gbf_copy_slices: dst slices [dst_s0, dst_s0 + count) = scale * src slices
+ * [src_s0, src_s0 + count) for every 4D site and rhs (g.separate / g.merge
+ * along the fifth dimension); the operators may differ in Ls, not in
+ * precision, 4D geometry or n_rhs.  nhalves: 1 one checkerboard, 2 full. */
+int gbf_chiral_shift(gbf_op* op, const void* src, void* dst, int offset, int nhalves, void* stream);
+int gbf_copy_slices(gbf_op* dst_op, void* dst, int dst_s0, gbf_op* src_op, const void* src, int src_s0, int count,
+                    double scale, int nhalves, void* stream);
+
 /* Mode representation dst = sum_n left[n] <right[n], src> f[n]
  * (lib/gpt/algorithms/modes/matrix.py:31-56; the deflation inverter
  * lib/gpt/algorithms/inverter/deflate.py is left = right = eigenvectors,
