@@ -1,5 +1,7 @@
-"""NERSC gauge files (lib/gpt/core/io/nersc_io.py; the reference's round-trip
-test is tests/io/io.py:198-206: save, load, relative difference < 1e-14)."""
+"""Gauge files: NERSC (lib/gpt/core/io/nersc_io.py) and LIME containers
+(lib/gpt/core/io/lime_io: gpt's lime format and ILDG files with SciDAC
+checksums).  The reference's round-trip tests are tests/io/io.py:198-216
+(save, load, relative difference < 1e-14); here the round trips are exact."""
 import os
 
 import numpy as np
@@ -102,3 +104,100 @@ def test_loaded_field_gives_the_same_operator(tmp_path):
     x[:] = s
     y[:] = s
     assert np.array_equal(a.M(x)[:], b.M(y)[:])
+
+
+# ---------------------------------------------------------------------------
+# LIME containers: gpt's lime format (the reference's round trip,
+# tests/io/io.py:208-216) and ILDG files (lime_io/load.py ildg-format branch)
+# ---------------------------------------------------------------------------
+def _lime_rec(tag, data):
+    import struct
+
+    h = struct.pack(">LHHQ", 0x456789AB, 1, 0xC000, len(data)) + tag.encode() + b"\0" * (128 - len(tag))
+    return h + data + b"\0" * ((8 - len(data) % 8) % 8)
+
+
+def _scidac_ref(site_bytes):
+    """Independent statement of the SciDAC checksum (lime_io/scidac.py:23-33)
+    with binascii and Python integers."""
+    import binascii
+
+    a = b = 0
+    for i, row in enumerate(site_bytes):
+        c = binascii.crc32(bytes(row)) & 0xFFFFFFFF
+        for m, acc in ((29, "a"), (31, "b")):
+            k = i % m
+            r = ((c << k) | (c >> (32 - k))) & 0xFFFFFFFF
+            if acc == "a":
+                a ^= r
+            else:
+                b ^= r
+    return a, b
+
+
+def test_lime_round_trip_is_exact(tmp_path):
+    U = _field(seed=21)
+    fn = str(tmp_path / "lime.0000")
+    g.save(fn, U, g.format.lime())
+    V = g.load(fn)
+    assert V.grid.fdimensions == U.grid.fdimensions and V.grid.precision is g.double
+    assert np.array_equal(V.host(), U.host())
+    assert V.metadata["otype"].startswith("ot_matrix_su_n_fundamental_group(3)")
+
+
+@pytest.mark.parametrize("bits", [64, 32])
+def test_ildg_round_trip(tmp_path, bits):
+    U = _field(seed=22)
+    fn = str(tmp_path / f"ildg{bits}")
+    g.save(fn, U, g.format.ildg(precision=bits))
+    V = g.load(fn)
+    assert V.grid.precision is (g.double if bits == 64 else g.single)
+    if bits == 64:
+        assert np.array_equal(V.host(), U.host())
+    else:
+        assert np.abs(V.host() - U.host()).max() < 1e-6
+
+
+def test_hand_built_ildg_file_with_namespaces_and_extra_records(tmp_path):
+    """An ILDG file as other writers produce it (namespaced XML, xlf-info and
+    lfn records, checksum written before the data), checked with an
+    independent statement of the SciDAC checksum."""
+    U = _field(dims=(4, 2, 2, 6), seed=23)
+    d = U.grid.fdimensions
+    data = np.ascontiguousarray(np.transpose(U.host(), (1, 0, 2, 3))).view(np.float64).astype(">f8")
+    site_bytes = data.view(np.uint8).reshape(int(np.prod(d)), -1)
+    a, b = _scidac_ref(site_bytes)
+    assert (a, b) == gio.scidac_checksums(site_bytes)
+    fmt = (f'<?xml version="1.0" encoding="UTF-8"?><ildgFormat xmlns="http://www.lqcd.org/ildg" '
+           f'xmlns:xsi="http://www.w3.org/2001/XMLSchema-instance"><version>1.0</version><field>su3gauge</field>'
+           f'<precision>64</precision><lx>{d[0]}</lx><ly>{d[1]}</ly><lz>{d[2]}</lz><lt>{d[3]}</lt></ildgFormat>')
+    cs = f"<?xml version='1.0'?><scidacChecksum><version>1.0</version><suma>{a:x}</suma><sumb>{b:x}</sumb></scidacChecksum>"
+    blob = (_lime_rec("xlf-info", b"plaquette = 0.5\n") + _lime_rec("ildg-format", fmt.encode())
+            + _lime_rec("scidac-checksum", cs.encode()) + _lime_rec("ildg-data-lfn", b"lfn://test/1")
+            + _lime_rec("ildg-binary-data", data.tobytes()))
+    fn = str(tmp_path / "ext.ildg")
+    open(fn, "wb").write(blob)
+    V = g.load(fn)
+    assert V.grid.fdimensions == list(d) and np.array_equal(V.host(), U.host())
+
+
+def test_corrupt_lime_files_are_rejected(tmp_path):
+    U = _field(seed=24)
+    fn = str(tmp_path / "ck.ildg")
+    g.save(fn, U, g.format.ildg())
+    raw = bytearray(open(fn, "rb").read())
+    i = raw.index(b"ildg-binary-data") + 128 + 100  # inside the binary data
+    raw[i] ^= 0x01
+    bad = str(tmp_path / "bad.ildg")
+    open(bad, "wb").write(bytes(raw))
+    with pytest.raises(ValueError, match="checksum"):
+        g.load(bad)
+    short = str(tmp_path / "short.ildg")
+    open(short, "wb").write(open(fn, "rb").read()[:-4096])
+    with pytest.raises(ValueError, match="truncated"):
+        g.load(short)
+    other = str(tmp_path / "prop.lime")
+    fmt = b"<ildgFormat><version>1.0</version><field>diracFermion</field><precision>64</precision></ildgFormat>"
+    open(other, "wb").write(_lime_rec("ildg-format", fmt) + _lime_rec("ildg-binary-data", b"\0" * 64))
+    with pytest.raises(NotImplementedError):
+        g.load(other)
