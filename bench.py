@@ -50,15 +50,19 @@ def parse():
     ap.add_argument("--dims", type=str, default=None, help="override lattice, e.g. 16,16,16,16 (tests only)")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-dhop-benchmark", action="store_true",
+                    help="c2: skip the reference's Dslash benchmark (Mobius Dhop 64.32.32.32 Ls 12) after the timed region")
     ap.add_argument("--profile-dslash", action="store_true",
                     help="profiling case: one operator only, one eo2_ne CG of 12 iterations")
     ap.add_argument("--profile-precision", default="single", choices=["single", "double", "double_float", "half"],
                     help="precision of the --profile-dslash operator")
     ap.add_argument("--profile-mobius", action="store_true",
                     help="profiling case: FP32 mobius 12^3x24 Ls 12 with 12 packed rhs, 12 CG iterations")
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "next", "dslash"],
                     help="c2 (default): wilson_clover 32^4 mixed vs plain; c1: wilson_clover 8^4; c3: mobius "
-                         "16^3x32 Ls=12, 12 point sources; c4: mobius 32^3x64 Ls=16, 12 sources; c5: serving stream")
+                         "16^3x32 Ls=12, 12 point sources; c4: mobius 32^3x64 Ls=16, 12 sources; c5: serving stream; "
+                         "next: the solver layers, operators and IO beyond the hot path; dslash: the reference's "
+                         "Dslash benchmark (Mobius Dhop, 64.32.32.32, Ls 12)")
     ap.add_argument("--requests", type=int, default=40, help="c5: number of requests")
     ap.add_argument("--inner", default="single", choices=["single", "half"], help="c3/c4 inner precision")
     ap.add_argument("--rhs-group", type=int, default=0, help="c4: right-hand sides solved together (0: auto)")
@@ -340,6 +344,253 @@ def run_c1(args):
     line = _common_line(METRIC, args.steps / (total_ms / 1000.0), "solves/s", args, 1, total_ms, cfg, "f64",
                         {"M_application_us": m_us, "M_vs_oracle_rel": m_err, "cg_iterations": cg.last.iterations,
                          "true_residual_oracle": tres})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# published numbers of the reference's own Dslash benchmark (benchmarks/dslash.py,
+# Mobius Dhop on 64.32.32.32, Ls 12, one node of 4 A100-SXM4-40GB:
+# benchmarks/reference/juwels_booster/dslash_n1.txt:57-64, 67-74)
+DHOP_PUBLISHED = {"single": {"gflops": 11325.46, "eff_gbs": 7824.86},
+                  "double": {"gflops": 5749.77, "eff_gbs": 7945.14},
+                  "hardware": "4x A100-SXM4-40GB (one JUWELS Booster node)"}
+
+
+def dwf_dhop_benchmark(reps=None):
+    """The reference's headline benchmark (benchmarks/dslash.py) on one GPU:
+    Mobius (mass 0.08, M5 1.8, b 1.5, c 0.5, Ls 12, periodic) Dhop on the
+    full 5D field of a 64.32.32.32 lattice, N applications after 5 warm-up
+    ones; flops = 1320 per 5D site and 'effective GB/s' = (8*2*4*3 +
+    8*2*9/Ls + 2*4*3) reals per 5D site, the reference's models
+    (dslash.py:54-61).  The algorithmic GB/s beside them counts each
+    neighbour spinor once (L2 serves the eightfold reuse) and the links once
+    per 4D site."""
+    import torch
+
+    import gpt_gb300 as g
+
+    L = g.load()
+    dims, Ls = [64, 32, 32, 32], 12
+    reps = reps or {"single": 1000, "double": 50, "double_float": 200}
+    grid = g.grid(dims, g.double)
+    U = g.qcd.gauge.random_su3_device(grid, 0.5, 777)
+    params = dict(mass=0.08, M5=1.8, b=1.5, c=0.5, Ls=Ls, boundary_phases=[1.0, 1.0, 1.0, 1.0])
+    V = grid.gsites
+    sites = V * Ls
+    stream = torch.cuda.current_stream()
+    out = {"workload": "mobius Dhop, full 5D field, 64.32.32.32 Ls 12 (benchmarks/dslash.py)",
+           "published_reference": DHOP_PUBLISHED}
+    for name, prec, sb, lb in (("single", g.single, 96, 48), ("double_float", g.double_float, 192, 144),
+                               ("double", g.double, 192, 144)):
+        op = g.qcd.fermion.mobius(U, params)
+        op = op if prec is g.double else op.converted(prec)
+        src, dst = op.F_lattice(), op.F_lattice()
+        nat = torch.empty(V * Ls * 24, dtype=torch.float64, device="cuda")
+        g._lib.check(L.gbf_random_spinor(V * Ls * 12, 99, nat.data_ptr(), g.core.stream_ptr()))
+        g._lib.check(L.gbf_field_import(src.layout.op, nat.data_ptr(), src.ptr, 0, 1, g.core.stream_ptr()))
+        del nat
+        n = reps[name]
+        for _ in range(5):
+            op.Dhop.mat(dst, src)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            op.Dhop.mat(dst, src)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        wbytes = 8 if prec is not g.single else 4
+        eff = (8 * 2 * 4 * 3 + 8 * 2 * 9 / Ls + 2 * 4 * 3) * wbytes * sites
+        alg = (sb + sb + 8 * lb / Ls) * sites
+        r = {"applications": n, "ms_per_application": ms, "gflops": 1320.0 * sites / (ms / 1000.0) / 1e9,
+             "eff_gbs_reference_model": eff / (ms / 1000.0) / 1e9, "algorithmic_gbs": alg / (ms / 1000.0) / 1e9}
+        pub = DHOP_PUBLISHED.get("double" if name == "double_float" else name)
+        r["gflops_over_published_node"] = r["gflops"] / pub["gflops"]
+        out[name] = r
+        del op, src, dst
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_dslash_bench(args):
+    """--config dslash: the reference's own Dslash benchmark, one JSON line;
+    value = FP32 GFlop/s (the published figure's precision)."""
+    t0 = time.time()
+    r = dwf_dhop_benchmark()
+    line = {"metric": "DWF Dhop GFlop/s (benchmarks/dslash.py model, 1320 flop per 5D site)",
+            "value": r["single"]["gflops"], "unit": "GFlop/s", "n_gpus": 1, "higher_is_better": True,
+            "vs_baseline": r["single"]["gflops"] / DHOP_PUBLISHED["single"]["gflops"],
+            "vs_baseline_note": "published figure is one node of 4 A100 GPUs; here one GB300",
+            "dtype": "f32 (double and double-float alongside)", "data": "synthetic",
+            "config": {"workload": r["workload"], "lattice": [64, 32, 32, 32], "Ls": 12},
+            "seconds": time.time() - t0}
+    line.update({k: v for k, v in r.items() if k not in ("workload",)})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_next_rows(args):
+    """--config next: one measurement per row beyond the hot path, on
+    synthetic inputs (gauge exp(i eps H), Gaussian sources), CUDA-event
+    timing after warm-up.  Algorithmic bytes count every field once per
+    kernel (the hop: input spinor, 8 links, output, plus X and the site-local
+    terms), as for the main roofline figure."""
+    import tempfile
+
+    import torch
+
+    import gpt_gb300 as g
+    from gpt_gb300 import _lib, core
+
+    L = g.load()
+    stream = torch.cuda.current_stream()
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+
+    def timed(fn, n, warm=2):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    def gbs(nbytes, ms):
+        return {"ms": ms, "algorithmic_gbs": nbytes / (ms / 1000.0) / 1e9, "frac_of_hbm_peak": nbytes / (ms / 1000.0) / 1e9 / peak}
+
+    out = {}
+    rng = np.random.default_rng(3)
+    t_all = time.time()
+
+    # ---- twisted-mass vs Wilson-clover M (32^4, FP32 and FP64) ----
+    dims = [32, 32, 32, 32]
+    U = g.qcd.gauge.random_su3_device(g.grid(dims, g.double), 0.3, 11)
+    Vh = int(np.prod(dims)) // 2
+    src4 = rng.standard_normal((2 * Vh, 4, 3)) + 1j * rng.standard_normal((2 * Vh, 4, 3))
+    res = {}
+    for prec, sb, lb in ((g.single, 96, 48), (g.double, 192, 144)):
+        for kind in ("wilson_clover", "wilson_twisted_mass"):
+            if kind == "wilson_clover":
+                op = g.qcd.fermion.wilson_clover(U, dict(mass=0.05, csw_r=1.0, csw_t=1.0, boundary_phases=[1, 1, 1, -1]))
+                local_b = 3 * sb  # clover: 288 / 576 B per site
+            else:
+                op = g.qcd.fermion.wilson_twisted_mass(U, dict(mass=0.05, mu=0.1, boundary_phases=[1, 1, 1, -1]))
+                local_b = 0
+            op = op if prec is g.double else op.converted(prec)
+            x, y = op.F_lattice(), op.F_lattice()
+            x[:] = src4
+            ms = timed(lambda: op.M(y, x), 20)
+            # M on both parities: out = Dhop(in) + Mooee in, per output site
+            # in 8 neighbours once + 8 links + out + X (+ clover)
+            nb = 2 * Vh * (sb + 8 * lb + sb + sb + local_b)
+            res[f"{kind}_{prec.name}"] = gbs(nb, ms)
+    out["twisted_mass_M_32^4"] = res
+
+    # ---- zmobius vs mobius M (16^3x32, Ls 10, FP32) ----
+    dims5 = [16, 16, 16, 32]
+    U5 = g.qcd.gauge.random_su3_device(g.grid(dims5, g.double), 0.4, 12)
+    omega = [0.17661651536320583 + 0.14907774771612217j, 0.23027432016909377 - 0.03530801572584271j,
+             0.3368765581549033, 0.7305711010541054, 1.1686138337986505 + 0.3506492418109086j,
+             1.1686138337986505 - 0.3506492418109086j, 0.994175013717952, 0.5029903152251229,
+             0.23027432016909377 + 0.03530801572584271j, 0.17661651536320583 - 0.14907774771612217j]
+    qm = g.qcd.fermion.mobius(U5, dict(mass=0.01, M5=1.8, b=1.5, c=0.5, Ls=10, boundary_phases=[1, 1, 1, -1]))
+    qz = g.qcd.fermion.zmobius(U5, dict(mass=0.01, M5=1.8, b=1.0, c=0.0, omega=omega, boundary_phases=[1, 1, 1, -1]))
+    res = {}
+    for name, op in (("mobius", qm), ("zmobius", qz)):
+        o32 = op.converted(g.single)
+        x, y = o32.F_lattice(), o32.F_lattice()
+        res[name + "_single_M_ms"] = timed(lambda: o32.M(y, x), 20)
+    res["zmobius_over_mobius"] = res["zmobius_single_M_ms"] / res["mobius_single_M_ms"]
+    out["zmobius_M_16^3x32_Ls10"] = res
+
+    # ---- multi-shift CG (Wilson-clover 24^4, FP64, 8 shifts) vs 8 single-shift solves ----
+    d24 = [24, 24, 24, 24]
+    U24 = g.qcd.gauge.random_su3_device(g.grid(d24, g.double), 0.3, 13)
+    w24 = g.qcd.fermion.wilson_clover(U24, dict(mass=0.1, csw_r=1.0, csw_t=1.0, boundary_phases=[1, 1, 1, -1]))
+    Mpc = g.qcd.fermion.preconditioner.eo2_ne()(w24).Mpc
+    b = w24.F_lattice(core.odd)
+    F = w24.F_lattice()
+    F[:] = rng.standard_normal((int(np.prod(d24)), 4, 3)) + 1j * rng.standard_normal((int(np.prod(d24)), 4, 3))
+    b.tensor.copy_(F.half(core.odd).tensor)
+    shifts = [1e-4, 3e-4, 1e-3, 3e-3, 1e-2, 3e-2, 0.1, 0.3]
+    inv = g.algorithms.inverter
+    ms_all = inv.multi_shift_cg({"eps": 1e-8, "maxiter": 5000, "shifts": shifts})
+    msx = ms_all(Mpc)
+    t_multi = timed(lambda: msx(b), 2, warm=1)
+    it_multi = ms_all.last.iterations
+    singles = [inv.multi_shift_cg({"eps": 1e-8, "maxiter": 5000, "shifts": [s]}) for s in shifts]
+    sx = [m(Mpc) for m in singles]
+    t_single = timed(lambda: [m(b) for m in sx], 1, warm=1)
+    out["multi_shift_cg_24^4_fp64_8_shifts"] = {
+        "ms_per_multishift_solve": t_multi, "iterations": it_multi, "ms_for_8_single_shift_solves": t_single,
+        "iterations_single": [m.last.iterations for m in singles], "speedup": t_single / t_multi}
+
+    # ---- deflation kernels: mode matrix with 32 modes on a 32^4 FP32 half field ----
+    w32 = g.qcd.fermion.wilson_clover(U, dict(mass=0.05, csw_r=1.0, csw_t=1.0, boundary_phases=[1, 1, 1, -1])).converted(g.single)
+    nev = 32
+    modes = [w32.F_lattice(core.odd) for _ in range(nev)]
+    for m_ in modes:
+        m_.tensor.copy_(torch.randint(0, 255, m_.tensor.shape, dtype=torch.uint8, device="cuda") & 0x3F)
+    src = w32.F_lattice(core.odd)
+    src.tensor.copy_(modes[0].tensor)
+    mm = g.algorithms.modes.matrix(modes, modes, list(np.linspace(0.1, 1.0, nev)), lambda v: 1.0 / v)
+    dst = w32.F_lattice(core.odd)
+    t_modes = timed(lambda: mm(dst, src), 5)
+    hb = w32.F_layout.half_bytes()
+    blocks = (nev + 7) // 8
+    nbytes = (nev + blocks) * hb + (nev + blocks + (blocks - 1)) * hb
+    out["deflation_mode_matrix_32^4_fp32_32_modes"] = gbs(nbytes, t_modes)
+
+    # ---- MADWF moves and a MADWF solve (16^3x32: Mobius Ls 12 outer, zmobius Ls 10 inner) ----
+    qm12 = g.qcd.fermion.mobius(U5, dict(mass=0.01, M5=1.8, b=1.5, c=0.5, Ls=12, boundary_phases=[1, 1, 1, -1]))
+    q32 = qm12.converted(g.single)
+    a, c_ = q32.F_lattice(), q32.F_lattice()
+    t_shift = timed(lambda: L.gbf_chiral_shift(a.layout.op, a.ptr, c_.ptr, 1, 2, core.stream_ptr()), 20)
+    out["madwf_chiral_shift_16^3x32_Ls12_fp32"] = gbs(2 * a.tensor.numel(), t_shift)
+    pc = g.qcd.fermion.preconditioner
+    inner_cg = inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": 1e-5, "maxiter": 4000}))
+    qz32 = qz.converted(g.single)
+    madwf = inv.defect_correcting(inv.mixed_precision(pc.mixed_dwf(inner_cg, inner_cg, qz32), g.single, g.double),
+                                  eps=1e-8, maxiter=30)
+    plain = inv.defect_correcting(inv.mixed_precision(inner_cg, g.single, g.double), eps=1e-8, maxiter=30)
+    S = qm12.U_lattice()
+    S[:] = rng.standard_normal((int(np.prod(dims5)), 4, 3)) + 1j * rng.standard_normal((int(np.prod(dims5)), 4, 3))
+    res = {}
+    for name, slv in (("madwf_zmobius_Ls10_inner", madwf), ("mixed_precision_cg", plain)):
+        prop = qm12.propagator(slv)
+        t0 = time.time()
+        x4 = prop(S)
+        torch.cuda.synchronize()
+        res[name] = {"s_per_solve": time.time() - t0, "outer_corrections": len(slv.history)}
+    out["madwf_solve_16^3x32_mobius_Ls12_to_1e-8"] = res
+
+    # ---- gauge-field IO (32^4 FP64, 604 MB) ----
+    H = U.host()
+    nbytes = H.nbytes
+    res = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name, fmt in (("nersc", g.format.nersc()), ("ildg", g.format.ildg()), ("lime", g.format.lime())):
+            fn = os.path.join(d, name)
+            t0 = time.time()
+            g.save(fn, U, fmt)
+            t1 = time.time()
+            V = g.load(fn)
+            t2 = time.time()
+            assert np.array_equal(V.host(), H)
+            res[name] = {"save_MBps": nbytes / (t1 - t0) / 1e6, "load_MBps": nbytes / (t2 - t1) / 1e6}
+            os.remove(fn)
+    out["gauge_io_32^4_fp64"] = res
+
+    line = {"metric": "rows beyond the hot path: kernel GB/s, solver speed-ups, IO MB/s", "value": None,
+            "unit": None, "n_gpus": 1, "data": "synthetic", "config": {"workload": "see each entry"},
+            "block_cg": "measured by --config c3 --solver block_cg", "seconds": time.time() - t_all}
+    line.update(out)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -768,6 +1019,11 @@ def run_gbf(args, dims):
                          f"corrections ({spent:.1f} s of CPU work)"}
         del op_o
 
+    # ---- the reference's own Dslash benchmark (benchmarks/dslash.py), after the timed region ----
+    dhop = None
+    if world == 1 and not args.no_dhop_benchmark:
+        dhop = dwf_dhop_benchmark()
+
     p = sorted(step_ms)
     line = {
         "metric": METRIC,
@@ -815,6 +1071,7 @@ def run_gbf(args, dims):
             "mixed_single_inner": {"solves_per_s": world * 1000.0 / mixed_dd_ms, "ms_per_solve": mixed_dd_ms,
                                    "true_residual_fp64": mixed_dd_true},
         },
+        "reference_dslash_benchmark": dhop,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -836,6 +1093,10 @@ def main():
         return run_mobius_config(args, args.config)
     if args.impl != "reference" and args.config == "c5":
         return run_c5(args)
+    if args.impl != "reference" and args.config == "next":
+        return run_next_rows(args)
+    if args.impl != "reference" and args.config == "dslash":
+        return run_dslash_bench(args)
     if args.impl == "reference":
         return run_reference(args, dims)
     return run_gbf(args, dims)

@@ -129,8 +129,9 @@ struct gbf_op {
   int ms_count = 0;
   // reduction partials: capacity of `partial` in double2 entries
   long long partial_cap = 0;
-  // mode representation: inner products of one block of modes (device)
+  // mode representation: inner products of the modes (device), capacity
   double2* mode_dev = nullptr;
+  int mode_cap = 0;
 
   size_t half() const { return (size_t)half_bytes(prec, g.N); }
   // workspace half field i; halves 2k and 2k+1 are one contiguous full field,
@@ -1320,29 +1321,36 @@ int gbf_modes_apply(gbf_op* op, const void* const* left, const void* const* righ
       if (left[i] == dst) throw Fail(GBF_E_ARG, "dst must not be a mode");
     }
     ensure_ws(op);
-    if (!op->mode_dev) op->mode_dev = (double2*)dmalloc(kModeBlock * sizeof(double2));
+    if (op->mode_cap < 2 * n) {
+      cudaFree(op->mode_dev);
+      op->mode_dev = nullptr;
+      op->mode_dev = (double2*)dmalloc((size_t)2 * n * sizeof(double2));
+      op->mode_cap = 2 * n;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     const size_t h = op->half();
-    // w_n = f_n <right_n, src>, summed over the halves
-    std::vector<std::complex<double>> w(n, 0.0);
-    for (int i0 = 0; i0 < n; i0 += kModeBlock) {
-      const int m = std::min(kModeBlock, n - i0);
-      for (int hf = 0; hf < nhalves; ++hf) {
+    // <right_n, src> per half, every block of modes on the stream, one read back
+    for (int hf = 0; hf < nhalves; ++hf) {
+      for (int i0 = 0; i0 < n; i0 += kModeBlock) {
+        const int m = std::min(kModeBlock, n - i0);
         ModeDotArgs a{};
         for (int j = 0; j < m; ++j) a.v[j] = (const char*)right[i0 + j] + hf * h;
         a.n = m;
         a.src = (const char*)src + hf * h;
         a.partial = op->partial;
         a.counter = op->counter;
-        a.out = op->mode_dev;
+        a.out = op->mode_dev + (size_t)hf * n + i0;
         CK(launch_mode_dot(op->prec, op->g, a, op->partial_cap, s));
         count_launch();
-        double2 c[kModeBlock];
-        CK(cudaMemcpyAsync(c, op->mode_dev, m * sizeof(double2), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        for (int j = 0; j < m; ++j) w[i0 + j] += std::complex<double>(c[j].x, c[j].y);
       }
     }
+    std::vector<double2> c((size_t)nhalves * n);
+    CK(cudaMemcpyAsync(c.data(), op->mode_dev, c.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    // w_n = f_n <right_n, src>, the halves summed in order
+    std::vector<std::complex<double>> w(n, 0.0);
+    for (int hf = 0; hf < nhalves; ++hf)
+      for (int i = 0; i < n; ++i) w[i] += std::complex<double>(c[(size_t)hf * n + i].x, c[(size_t)hf * n + i].y);
     for (int i = 0; i < n; ++i) w[i] *= std::complex<double>(f[2 * i], f[2 * i + 1]);
     // dst = sum_n w_n left_n, kModeBlock modes per pass
     for (int hf = 0; hf < nhalves; ++hf) {

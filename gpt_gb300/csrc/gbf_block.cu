@@ -380,40 +380,47 @@ namespace gbf {
 // of up to kModeBlock of them through one pass over the sites.
 // ---------------------------------------------------------------------------
 
-// out[j] = sum_sites conj(v_j) . src: per-site products in the arithmetic
-// precision summed per thread in FP64, FP64 block sums in a fixed order, the
-// last block sums the [block][j] partials in block order (deterministic).
-// bytes/site: src once + every v_j once.
-template <int P>
+// out[j] = sum_sites conj(v_j) . src: products and the per-thread sums over
+// the thread's sites in the arithmetic precision (a thread handles a few
+// sites: the grid is one wave of resident blocks), FP64 block sums in a fixed
+// order, the last block sums the [block][j] partials in block order
+// (deterministic).  NM = kModeBlock for full blocks (no predication), 0 for
+// a run-time count a.n < kModeBlock.  bytes/site: src once + every v_j once.
+template <int P, int NM>
 __global__ void __launch_bounds__(256) mode_dot_kernel(const Geo g, const ModeDotArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
   __shared__ double sm[64];
   const int t = threadIdx.x;
-  double re[kModeBlock], im[kModeBlock];
+  const int nm = NM ? NM : a.n;
+  R re[kModeBlock], im[kModeBlock];
 #pragma unroll
-  for (int j = 0; j < kModeBlock; ++j) re[j] = im[j] = 0.0;
+  for (int j = 0; j < kModeBlock; ++j) re[j] = im[j] = rzero<R>();
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long n = (long long)blockIdx.x * blockDim.x + t; n < g.N; n += stride) {
     V s[12];
     load_spinor<P>(a.src, g.N, n, s);
 #pragma unroll
+    for (int k = 0; k < 12; ++k) nrm<R>(s[k]);
+#pragma unroll
     for (int j = 0; j < kModeBlock; ++j) {
-      if (j < a.n) {
+      if (NM || j < nm) {
         V v[12];
         load_spinor<P>(a.v[j], g.N, n, v);
-        double dr, di;
-        site_dot<R>(v, s, dr, di);
-        re[j] += dr;
-        im[j] += di;
+#pragma unroll
+        for (int k = 0; k < 12; ++k) nrm<R>(v[k]);
+        R dr, di;
+        site_dot_r<R>(v, s, dr, di);
+        re[j] = re[j] + dr;
+        im[j] = im[j] + di;
       }
     }
   }
 #pragma unroll
   for (int j = 0; j < kModeBlock; ++j) {
-    if (j < a.n) {
-      const double2 b = block_sum_shfl(re[j], im[j], sm);
-      if (t == 0) a.partial[(size_t)blockIdx.x * a.n + j] = b;
+    if (NM || j < nm) {
+      const double2 b = block_sum_shfl((double)re[j], (double)im[j], sm);
+      if (t == 0) a.partial[(size_t)blockIdx.x * nm + j] = b;
     }
   }
   __threadfence();
@@ -423,10 +430,10 @@ __global__ void __launch_bounds__(256) mode_dot_kernel(const Geo g, const ModeDo
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  if (t < a.n) {
+  if (t < nm) {
     double sr = 0.0, si = 0.0;
     for (unsigned b = 0; b < gridDim.x; ++b) {
-      const double2 v = __ldcg(a.partial + (size_t)b * a.n + t);
+      const double2 v = __ldcg(a.partial + (size_t)b * nm + t);
       sr += v.x;
       si += v.y;
     }
@@ -436,11 +443,16 @@ __global__ void __launch_bounds__(256) mode_dot_kernel(const Geo g, const ModeDo
 }
 
 // out = (accumulate ? out : 0) + sum_j w_j v_j, complex weights rounded to
-// the arithmetic precision.  bytes/site: every v_j once, out written (+ read).
-template <int P>
+// the arithmetic precision once per thread.  bytes/site: every v_j once, out
+// written (+ read).
+template <int P, int NM>
 __global__ void __launch_bounds__(256) mode_axpy_kernel(const Geo g, const ModeAxpyArgs a) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
+  const int nm = NM ? NM : a.n;
+  V w[kModeBlock];
+#pragma unroll
+  for (int j = 0; j < kModeBlock; ++j) w[j] = mk<R>((R)a.w[j].x, (R)a.w[j].y);
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < g.N; n += stride) {
     V o[12];
@@ -450,25 +462,26 @@ __global__ void __launch_bounds__(256) mode_axpy_kernel(const Geo g, const ModeA
 #pragma unroll
       for (int k = 0; k < 12; ++k) o[k] = cz<R>();
     }
-#pragma unroll 1
-    for (int j = 0; j < a.n; ++j) {
-      V v[12];
-      load_spinor<P>(a.v[j], g.N, n, v);
-      const V w = mk<R>((R)a.w[j].x, (R)a.w[j].y);
 #pragma unroll
-      for (int k = 0; k < 12; ++k) {
-        nrm<R>(v[k]);
-        o[k] = cmadd<R>(o[k], w, v[k]);
-        nrm<R>(o[k]);
+    for (int j = 0; j < kModeBlock; ++j) {
+      if (NM || j < nm) {
+        V v[12];
+        load_spinor<P>(a.v[j], g.N, n, v);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+          nrm<R>(v[k]);
+          o[k] = cmadd<R>(o[k], w[j], v[k]);
+          nrm<R>(o[k]);
+        }
       }
     }
     store_spinor<P>(a.out, g.N, n, o);
   }
 }
 
-template <int P>
+template <int P, int NM>
 static cudaError_t launch_mode_dot_t(const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st) {
-  auto k = mode_dot_kernel<P>;
+  auto k = mode_dot_kernel<P, NM>;
   const int bd = 256;
   long long nb = reduce_grid((g.N + bd - 1) / bd, 1, resident_blocks((const void*)k, bd, 0));
   if (nb * a.n > max_partials) nb = max_partials / a.n;
@@ -477,30 +490,41 @@ static cudaError_t launch_mode_dot_t(const Geo& g, const ModeDotArgs& a, long lo
   return cudaGetLastError();
 }
 
+template <int P>
+static cudaError_t launch_mode_dot_p(const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st) {
+  return a.n == kModeBlock ? launch_mode_dot_t<P, kModeBlock>(g, a, max_partials, st)
+                           : launch_mode_dot_t<P, 0>(g, a, max_partials, st);
+}
+
 cudaError_t launch_mode_dot(int P, const Geo& g, const ModeDotArgs& a, long long max_partials, cudaStream_t st) {
   if (a.n < 1 || a.n > kModeBlock) return cudaErrorInvalidValue;
-  if (P == P64) return launch_mode_dot_t<P64>(g, a, max_partials, st);
-  if (P == P32) return launch_mode_dot_t<P32>(g, a, max_partials, st);
-  if (P == P16) return launch_mode_dot_t<P16>(g, a, max_partials, st);
-  if (P == PDD) return launch_mode_dot_t<PDD>(g, a, max_partials, st);
+  if (P == P64) return launch_mode_dot_p<P64>(g, a, max_partials, st);
+  if (P == P32) return launch_mode_dot_p<P32>(g, a, max_partials, st);
+  if (P == P16) return launch_mode_dot_p<P16>(g, a, max_partials, st);
+  if (P == PDD) return launch_mode_dot_p<PDD>(g, a, max_partials, st);
   return cudaErrorInvalidValue;
 }
 
-template <int P>
+template <int P, int NM>
 static cudaError_t launch_mode_axpy_t(const Geo& g, const ModeAxpyArgs& a, cudaStream_t st) {
-  auto k = mode_axpy_kernel<P>;
+  auto k = mode_axpy_kernel<P, NM>;
   const int bd = 256;
   const long long nb = reduce_grid((g.N + bd - 1) / bd, 1, resident_blocks((const void*)k, bd, 0));
   k<<<(unsigned)nb, bd, 0, st>>>(g, a);
   return cudaGetLastError();
 }
 
+template <int P>
+static cudaError_t launch_mode_axpy_p(const Geo& g, const ModeAxpyArgs& a, cudaStream_t st) {
+  return a.n == kModeBlock ? launch_mode_axpy_t<P, kModeBlock>(g, a, st) : launch_mode_axpy_t<P, 0>(g, a, st);
+}
+
 cudaError_t launch_mode_axpy(int P, const Geo& g, const ModeAxpyArgs& a, cudaStream_t st) {
   if (a.n < 0 || a.n > kModeBlock) return cudaErrorInvalidValue;
-  if (P == P64) return launch_mode_axpy_t<P64>(g, a, st);
-  if (P == P32) return launch_mode_axpy_t<P32>(g, a, st);
-  if (P == P16) return launch_mode_axpy_t<P16>(g, a, st);
-  if (P == PDD) return launch_mode_axpy_t<PDD>(g, a, st);
+  if (P == P64) return launch_mode_axpy_p<P64>(g, a, st);
+  if (P == P32) return launch_mode_axpy_p<P32>(g, a, st);
+  if (P == P16) return launch_mode_axpy_p<P16>(g, a, st);
+  if (P == PDD) return launch_mode_axpy_p<PDD>(g, a, st);
   return cudaErrorInvalidValue;
 }
 

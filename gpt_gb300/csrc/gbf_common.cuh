@@ -320,10 +320,8 @@ template <> __device__ __forceinline__ void load_link<L32, float>(const void* li
 #pragma unroll
   for (int k = 0; k < 9; ++k) u[k] = __ldg(b + (o + (unsigned)k * (unsigned)Vh));
 }
-template <> __device__ __forceinline__ void load_link<L32R, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
-  const float4* b = reinterpret_cast<const float4*>(links);
-  const unsigned o = (unsigned)((p * 4 + mu) * 3) * (unsigned)Vh + (unsigned)cb;
-  float4 a0 = __ldg(b + o), a1 = __ldg(b + (o + (unsigned)Vh)), a2 = __ldg(b + (o + 2u * (unsigned)Vh));
+// SU(3) link from its first two rows (three float4): row 2 = conj(row0 x row1)
+__device__ __forceinline__ void link12_rebuild(const float4 a0, const float4 a1, const float4 a2, float2 (&u)[9]) {
   u[0] = make_float2(a0.x, a0.y); u[1] = make_float2(a0.z, a0.w); u[2] = make_float2(a1.x, a1.y);
   u[3] = make_float2(a1.z, a1.w); u[4] = make_float2(a2.x, a2.y); u[5] = make_float2(a2.z, a2.w);
   // row2 = conj(row0 x row1)
@@ -333,6 +331,11 @@ template <> __device__ __forceinline__ void load_link<L32R, float>(const void* l
                      -(u[2].x * u[3].y + u[2].y * u[3].x - (u[0].x * u[5].y + u[0].y * u[5].x)));
   u[8] = make_float2(u[0].x * u[4].x - u[0].y * u[4].y - (u[1].x * u[3].x - u[1].y * u[3].y),
                      -(u[0].x * u[4].y + u[0].y * u[4].x - (u[1].x * u[3].y + u[1].y * u[3].x)));
+}
+template <> __device__ __forceinline__ void load_link<L32R, float>(const void* links, int Vh, int p, int mu, int cb, float2 (&u)[9]) {
+  const float4* b = reinterpret_cast<const float4*>(links);
+  const unsigned o = (unsigned)((p * 4 + mu) * 3) * (unsigned)Vh + (unsigned)cb;
+  link12_rebuild(__ldg(b + o), __ldg(b + (o + (unsigned)Vh)), __ldg(b + (o + 2u * (unsigned)Vh)), u);
 }
 
 // ---------------------------------------------------------------------------
