@@ -56,6 +56,9 @@ def parse():
                     help="profiling case: one operator only, one eo2_ne CG of 12 iterations")
     ap.add_argument("--profile-precision", default="single", choices=["single", "double", "double_float", "half"],
                     help="precision of the --profile-dslash operator")
+    ap.add_argument("--profile-next", action="store_true",
+                    help="profiling case of the kernels beyond the hot path: mode matrix, chiral shift, slice copy, "
+                         "multi-shift update, block-CG Gram and linear combination (a few GB on the device)")
     ap.add_argument("--profile-mobius", action="store_true",
                     help="profiling case: FP32 mobius 12^3x24 Ls 12 with 12 packed rhs, 12 CG iterations")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "next", "dslash"],
@@ -427,6 +430,76 @@ def run_dslash_bench(args):
             "seconds": time.time() - t0}
     line.update({k: v for k, v in r.items() if k not in ("workload",)})
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile_next(args):
+    """Profiling case of the kernels beyond the hot path, each launched a few
+    times on inputs larger than L2: mode matrix (16 modes, Wilson 24^4 FP32
+    half fields, 16 MB each), chiral shift and slice copy (Mobius 16^3x32
+    Ls 12 FP32 full fields, 151 MB), multi-shift CG (Wilson-clover 24^4 FP64,
+    4 shifts, 10 iterations), block CG (Mobius 12^3x24 Ls 12, 4 packed rhs,
+    FP32, 5 iterations).  Prints the algorithmic bytes per launch of each."""
+    import torch
+
+    import gpt_gb300 as g
+    from gpt_gb300 import core
+
+    L = g.load()
+    rng = np.random.default_rng(5)
+    out = {}
+    d24 = [24, 24, 24, 24]
+    U24 = g.qcd.gauge.random_su3_device(g.grid(d24, g.double), 0.3, 21)
+    wc = g.qcd.fermion.wilson_clover(U24, dict(mass=0.1, csw_r=1.0, csw_t=1.0, boundary_phases=[1, 1, 1, -1]))
+    w32 = wc.converted(g.single)
+    modes = [w32.F_lattice(core.odd) for _ in range(16)]
+    for m_ in modes:
+        m_.tensor.copy_(torch.randint(0, 255, m_.tensor.shape, dtype=torch.uint8, device="cuda") & 0x3F)
+    src, dst = w32.F_lattice(core.odd), w32.F_lattice(core.odd)
+    src.tensor.copy_(modes[1].tensor)
+    mm = g.algorithms.modes.matrix(modes, modes, list(np.linspace(0.1, 1.0, 16)), lambda v: 1.0 / v)
+    for _ in range(3):
+        mm(dst, src)
+    hb = w32.F_layout.half_bytes()
+    out["mode_dot_kernel_bytes"] = 9 * hb
+    out["mode_axpy_kernel_bytes"] = [9 * hb, 10 * hb]
+    d5 = [16, 16, 16, 32]
+    U5 = g.qcd.gauge.random_su3_device(g.grid(d5, g.double), 0.4, 22)
+    qm = g.qcd.fermion.mobius(U5, dict(mass=0.01, M5=1.8, b=1.5, c=0.5, Ls=12, boundary_phases=[1, 1, 1, -1])).converted(g.single)
+    qs = g.qcd.fermion.mobius(U5, dict(mass=0.01, M5=1.8, b=1.5, c=0.5, Ls=6, boundary_phases=[1, 1, 1, -1])).converted(g.single)
+    a, b = qm.F_lattice(), qm.F_lattice()
+    c = qs.F_lattice()
+    a.tensor.copy_(torch.randint(0, 255, a.tensor.shape, dtype=torch.uint8, device="cuda") & 0x3F)
+    for _ in range(3):
+        g._lib.check(L.gbf_chiral_shift(a.layout.op, a.ptr, b.ptr, 1, 2, core.stream_ptr()))
+        g._lib.check(L.gbf_copy_slices(c.layout.op, c.ptr, 0, a.layout.op, a.ptr, 3, 6, -1.0, 2, core.stream_ptr()))
+    out["chiral_shift_kernel_bytes_per_half"] = 2 * a.layout.half_bytes()
+    out["copy_slices_kernel_bytes_per_half"] = 2 * c.layout.half_bytes()
+    Mpc = g.qcd.fermion.preconditioner.eo2_ne()(wc).Mpc
+    F = wc.F_lattice()
+    V = int(np.prod(d24))
+    F[:] = rng.standard_normal((V, 4, 3)) + 1j * rng.standard_normal((V, 4, 3))
+    bsrc = F.half(core.odd)
+    ms = g.algorithms.inverter.multi_shift_cg({"eps": 1e-30, "maxiter": 10, "shifts": [0.01, 0.05, 0.2, 1.0]})
+    ms(Mpc)(bsrc)
+    out["multishift_kernel_bytes"] = (1 + 4 * 4) * wc.F_layout.half_bytes()
+    d3 = [12, 12, 12, 24]
+    U3 = g.qcd.gauge.random_su3_device(g.grid(d3, g.double), 0.4, 23)
+    qb = g.qcd.fermion.mobius_operator(U3, dict(Ls=12, b=1.5, c=0.5, M5=1.8, mass_plus=0.01, mass_minus=0.01,
+                                                boundary_phases=[1, 1, 1, -1], n_rhs=4), precision=g.single)
+    sb = qb.F_lattice()
+    nat = torch.empty(int(np.prod(d3)) * 12 * 24, dtype=torch.float64, device="cuda")
+    for k in range(4):
+        g._lib.check(L.gbf_random_spinor(int(np.prod(d3)) * 12 * 12, 60 + k, nat.data_ptr(), core.stream_ptr()))
+        g._lib.check(L.gbf_field_import(sb.layout.op, nat.data_ptr(), sb.ptr, k, 1, core.stream_ptr()))
+    xb = qb.F_lattice()
+    qb._solve_eo2ne_block_cg(xb, sb, 1e-30, 5)
+    hb5 = qb.F_layout.half_bytes()
+    out["gram_kernel_bytes"] = 2 * hb5
+    out["lincomb_kernel_bytes"] = 3 * hb5
+    out["lincomb2_kernel_bytes"] = 6 * hb5
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "kernels beyond the hot path", **out}))
     return 0
 
 
@@ -1087,6 +1160,8 @@ def main():
         return run_profile_case(args, dims)
     if args.profile_mobius:
         return run_profile_mobius(args)
+    if args.profile_next:
+        return run_profile_next(args)
     if args.impl != "reference" and args.config == "c1":
         return run_c1(args)
     if args.impl != "reference" and args.config in ("c3", "c4"):

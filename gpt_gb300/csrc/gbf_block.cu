@@ -112,14 +112,20 @@ __global__ void __launch_bounds__(256) gram_kernel(const Geo g, const void* A, c
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  for (int q = t; q < k * k; q += bd) {
+  // full warp w sums entries q = w, w + nw, ...: lane l adds blocks l,
+  // l + 32, ... in order, then a fixed shuffle tree (deterministic).  bd >= 129
+  // (block_size_for), so nw >= 4; a partial last warp takes no part.
+  const int lane = t & 31, nw = bd >> 5;
+  for (int q = t >> 5; q < k * k && (t >> 5) < nw; q += nw) {
     double re = 0.0, im = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) {
+    for (unsigned b = lane; b < gridDim.x; b += 32) {
       const double2 v = __ldcg(partial + (size_t)b * k * k + q);
       re += v.x;
       im += v.y;
     }
-    out[q] = make_double2(re, im);
+    re = warp_sum(re);
+    im = warp_sum(im);
+    if (lane == 0) out[q] = make_double2(re, im);
   }
   if (t == 0) *counter = 0u;
 }
@@ -430,14 +436,19 @@ __global__ void __launch_bounds__(256) mode_dot_kernel(const Geo g, const ModeDo
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  if (t < nm) {
+  // warp j sums mode j: lane l adds blocks l, l + 32, ... in order, then a
+  // fixed shuffle tree (deterministic); blockDim = 256 gives 8 warps
+  const int lane = t & 31, w = t >> 5;
+  if (w < nm) {
     double sr = 0.0, si = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-      const double2 v = __ldcg(a.partial + (size_t)b * nm + t);
+    for (unsigned b = lane; b < gridDim.x; b += 32) {
+      const double2 v = __ldcg(a.partial + (size_t)b * nm + w);
       sr += v.x;
       si += v.y;
     }
-    a.out[t] = make_double2(sr, si);
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) a.out[w] = make_double2(sr, si);
   }
   if (t == 0) *a.counter = 0u;
 }
