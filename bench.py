@@ -72,9 +72,10 @@ def parse():
     ap.add_argument("--with-plain", action="store_true",
                     help="c3: also time one plain FP64 and one plain double-float packed solve of the same sources")
     ap.add_argument("--cg-graph", type=int, default=0,
-                    help="c2: CG iterations per CUDA graph with a host convergence check between graphs "
-                         "(0: the whole CG loop on the device, one graph with a conditional while node; -1: no "
-                         "graphs, every kernel launched from the host, for per-kernel launch lists under ncu)")
+                    help="c2: CG iterations per CUDA graph with a host convergence check between graphs (0: the "
+                         "library default, 16; -1: the whole CG loop on the device, one graph with a conditional "
+                         "while node; -2: no graphs, every kernel launched from the host, for per-kernel launch "
+                         "lists under ncu)")
     ap.add_argument("--solver", default="cg", choices=["cg", "block_cg"],
                     help="c3/c4 inner solver: independent CG per packed rhs, or block CG over them")
     return ap.parse_args()
@@ -706,7 +707,12 @@ def run_c5(args):
                         {"p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "requests_per_s": s["requests_per_s"],
                          "failed": s["failed"], "max_true_residual": s["max_true_residual"], "gpu_launches": int(n1 - n0),
                          "clocks": clk, "serial_plain_fp64": {"solves_per_s": ss["solves_per_s"], "wall_s": swall,
-                                                               "max_true_residual": ss["max_true_residual"]},
+                                                               "max_true_residual": ss["max_true_residual"],
+                                                               "above_tol": [(r.rid, r.L, r.n_src, max(r.true_residual))
+                                                                             for r in serial if r.true_residual and
+                                                                             max(r.true_residual) > 1e-10]},
+                         "mixed_above_tol": [(r.rid, r.L, r.n_src, max(r.true_residual)) for r in res
+                                             if r.true_residual and max(r.true_residual) > 1e-10],
                          "speedup_vs_serial_plain": s["solves_per_s"] / ss["solves_per_s"] if ss["solves_per_s"] else None})
     print(json.dumps(line), flush=True)
     return 0
@@ -894,7 +900,7 @@ def run_gbf(args, dims):
     op = g.qcd.fermion.wilson_clover(U, params)
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
-    cg_loop = {"iterations_per_graph": max(0, args.cg_graph), "profile": args.cg_graph < 0}
+    cg_loop = {"iterations_per_graph": max(-1, args.cg_graph), "profile": args.cg_graph < -1}
     inner_cg = inv.cg({"eps": CFG["inner_tol"], "maxiter": 20000, **cg_loop})
     dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inner_cg), g.single, g.double),
                                eps=CFG["tol"], maxiter=100)
@@ -1128,8 +1134,9 @@ def run_gbf(args, dims):
         "plain_fp64": {"solves_per_s": world * 1000.0 / plain_ms, "ms_per_solve": plain_ms, "cg_iterations": plain_it,
                        "true_residual": plain_true, "true_residual_oracle": oracle_res.get("plain")},
         "mixed_over_plain": (value / world) / (1000.0 / plain_ms),
-        "cg_loop": ("device: one CUDA graph with a conditional while node" if args.cg_graph == 0 else
+        "cg_loop": ("host-checked CUDA graphs of 16 iterations" if args.cg_graph == 0 else
                     f"host-checked CUDA graphs of {args.cg_graph} iterations" if args.cg_graph > 0 else
+                    "device: one CUDA graph with a conditional while node" if args.cg_graph == -1 else
                     "no graphs: host launches with CUDA events (diagnostic)"),
         "dslash_fp32": {"hbm_gbs": achieved, "avg_launch_ms": d_ms},
         "dslash_fp64": {"algorithmic_gbs": fp64_gbs, "avg_launch_ms": d64_ms, "frac_of_hbm_peak": fp64_gbs / peak,

@@ -25,10 +25,11 @@ class cg:
         self.eps = p.get("eps", eps)
         self.maxiter = p.get("maxiter", maxiter)
         self.fail_if_not_converged = p.get("fail_if_not_converged", fail_if_not_converged)
-        # iterations_per_graph 0: the whole CG loop runs on the device (one CUDA
-        # graph with a conditional while node); K > 0: graphs of K iterations
-        # with a host convergence check between them.  profile: no graphs,
-        # every kernel launched from the host between CUDA events (diagnostic)
+        # iterations_per_graph K > 0: CUDA graphs of K iterations with a host
+        # convergence check between them; 0: the library's default K (16);
+        # -1: the whole CG loop on the device (one CUDA graph with a
+        # conditional while node), for single-threaded use.  profile: no
+        # graphs, every kernel launched from the host between CUDA events
         self.iterations_per_graph = p.get("iterations_per_graph", iterations_per_graph)
         self.profile = bool(p.get("profile", profile))
         self.history = []

@@ -27,6 +27,8 @@ using namespace gbf;
 static thread_local std::string g_err;
 static std::atomic<unsigned long long> g_launches{0};
 static inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+// CG iterations per host-checked graph launch when the caller passes 0
+static constexpr int kDefaultGraphIterations = 16;
 
 namespace {
 
@@ -1047,7 +1049,7 @@ bool cg_loop(gbf_op* op, cudaStream_t s, const gbf_cg_params* prm, double* kms, 
     for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
   }
   bool device_loop = false;
-  if (!prm->profile && prm->iterations_per_graph <= 0) {
+  if (!prm->profile && prm->iterations_per_graph < 0) {
     // ---- the whole CG loop on the device: a conditional while node whose
     // body is one iteration; the CG update kernel sets the loop condition to
     // !all_done (converged, maxiter reached or every rhs broken down), and
@@ -1093,7 +1095,7 @@ bool cg_loop(gbf_op* op, cudaStream_t s, const gbf_cg_params* prm, double* kms, 
     CK(cudaStreamSynchronize(s));
   }
   // ---- CG loop in graphs of K iterations, convergence checked by the host ----
-  const int K = prm->iterations_per_graph > 0 ? prm->iterations_per_graph : 8;
+  const int K = prm->iterations_per_graph > 0 ? prm->iterations_per_graph : kDefaultGraphIterations;
   if (!prm->profile && !device_loop && (!op->graph || op->graph_K != K)) {
     op->drop_graphs();
     cudaGraph_t gr;

@@ -209,7 +209,7 @@ def summarize(results, wall):
 # ---------------------------------------------------------------------------
 # the GPU executor
 # ---------------------------------------------------------------------------
-def gpu_executor(keep_solution=False, inner_tol=1e-5):
+def gpu_executor(keep_solution=False, inner_tol=1e-5, iterations_per_graph=0):
     """executor for Server: Wilson-clover (csw 1.0, phases [1,1,1,-1]) on a
     fresh device-generated gauge field; mixed = defect_correcting(
     mixed_precision(preconditioned(eo2_ne, cg(inner_tol))), single, double);
@@ -239,12 +239,15 @@ def gpu_executor(keep_solution=False, inner_tol=1e-5):
             pc = fermion.preconditioner
             if method == "mixed":
                 solver = inv.defect_correcting(
-                    inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": inner_tol, "maxiter": 20000})),
+                    inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": inner_tol, "maxiter": 20000,
+                                                                               "iterations_per_graph": iterations_per_graph})),
                                         core.single, core.double), eps=req.tol, maxiter=100)(op)
             else:
                 # eps bounds the eo2_ne normal residual; tol / 3 brings the true
                 # residual of M x = b below tol (eps = tol leaves about 2 tol)
-                solver = inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": req.tol / 3, "maxiter": 40000}))(op)
+                solver = inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": req.tol / 3, "maxiter": 40000,
+                                                                 "iterations_per_graph": iterations_per_graph,
+                                                                 "fail_if_not_converged": True}))(op)
             x = solver(src)
             r = op.F_lattice()
             op.M(r, x)

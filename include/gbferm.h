@@ -130,14 +130,19 @@ int gbf_convert(gbf_op* dst_op, void* dst, gbf_op* src_op, const void* src, doub
  * (lib/gpt/algorithms/inverter/preconditioned.py:32-54, cg.py:47-105,
  * lib/gpt/qcd/fermion/preconditioner/even_odd_sites.py:61-72): solves
  * M x = src for all packed right-hand sides with zero initial guess.  The CG
- * loop runs in a CUDA graph with device-resident scalars (see
+ * loop runs in CUDA graphs with device-resident scalars (see
  * iterations_per_graph). */
 typedef struct {
   double eps;
   int maxiter;
-  int iterations_per_graph; /* 0: the whole CG loop runs on the device (a CUDA graph with a
-                               conditional while node, no host round trip); K > 0: graphs of K
-                               iterations, convergence checked by the host between them */
+  int iterations_per_graph; /* K > 0: the CG loop runs as CUDA graphs of K iterations, the host
+                               checks convergence between graph launches (kernels of iterations
+                               past convergence return at once); 0: K = 16; -1: the whole loop
+                               on the device, one CUDA graph with a conditional while node and no
+                               host round trip.  Bitwise equal solutions in all modes.  With -1,
+                               2 of 160 solves that ran concurrently with solves of other
+                               operators on other host threads returned after zero iterations
+                               (reported as not converged); use it from one thread only. */
   int profile;              /* 1: no graphs; CUDA events time every kernel class (diagnostic run) */
 } gbf_cg_params;
 typedef struct {
@@ -183,7 +188,7 @@ int gbf_solve_eo2ne_multishift(gbf_op* op, const void* src, void* const* x, cons
  * starting from x as passed in (zero allowed) and overwriting it with the
  * solution; b = 0 gives x = 0.  Converged when |r|^2 <= eps^2 |b|^2 (checked
  * before the first iteration too); residual_sq = |r|^2 / |b|^2.  The loop
- * is the one of gbf_solve_eo2ne_cg (device loop, iterations_per_graph,
+ * is the one of gbf_solve_eo2ne_cg (graphs, iterations_per_graph,
  * profile).  This is the inner solve of inverter.sequence(deflate(...), cg)
  * (lib/gpt/algorithms/inverter/sequence.py:23-42). */
 int gbf_solve_normal_cg(gbf_op* op, const void* b, void* x, const gbf_cg_params* p, gbf_cg_result* res, void* stream);

@@ -365,9 +365,10 @@ def test_reductions_bitwise_deterministic():
 
 @pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1))])
 def test_device_loop_equals_host_checked_graphs(kind, params):
-    """The CG loop as one conditional-while graph (default), as host-checked
-    graphs of 8 iterations and as plain host launches (profile) runs the same
-    kernels: bitwise equal solutions and the same iteration count."""
+    """The CG loop as host-checked graphs (the default 16 and 8 iterations),
+    as one conditional-while graph on the device and as plain host launches
+    (profile) runs the same kernels: bitwise equal solutions and the same
+    iteration count."""
     dims = [4, 4, 4, 8]
     U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 33).U
     op = gpu_op(kind, U, dims, g.double, **params)
@@ -375,7 +376,7 @@ def test_device_loop_equals_host_checked_graphs(kind, params):
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
     out = []
-    for K, prof in ((0, False), (8, False), (0, False), (0, True)):
+    for K, prof in ((0, False), (8, False), (-1, False), (-1, False), (0, True)):
         cg = inv.cg({"eps": 1e-10, "maxiter": 2000, "iterations_per_graph": K, "profile": prof})
         x = inv.preconditioned(pc.eo2_ne(), cg)(op)(b)
         assert cg.last.converged
