@@ -10,7 +10,7 @@ memory and streams only.
 """
 from .core import (
     precision, double, single, half, double_float, even, odd, full, grid, layout, lattice, vspincolor,
-    norm2, inner_product, axpy, axpby, copy, convert,
+    norm2, inner_product, axpy, axpby, axpy_norm2, inner_product_norm2, copy, convert,
 )
 from . import _lib
 from . import qcd

@@ -104,6 +104,7 @@ def load():
         "gbf_eo2ne_reconstruct": (I, [P, P, P, P, P]),
         "gbf_modes_apply": (I, [P, PP, PP, DP, I, P, P, I, P]),
         "gbf_chiral_shift": (I, [P, P, P, I, I, P]),
+        "gbf_axpy_norm2": (I, [P, P, DP, DP, P, P, I, DP, P]),
         "gbf_copy_slices": (I, [P, P, I, P, P, I, I, ctypes.c_double, I, P]),
         "gbf_last_error": (ctypes.c_char_p, []),
         "gbf_stream_sync": (I, [P]),

@@ -287,6 +287,25 @@ def axpy(out, a, x, y):
     return axpby(out, a, x, 1.0, y)
 
 
+def axpy_norm2(out, a, x, y):
+    """gpt.axpy_norm2 (lib/gpt/core/transform.py:139-153): out = a x + y and
+    |out|^2 per rhs, in one fused pass (gbf_axpy_norm2)."""
+    n = _n(x)
+    a = _vec(a, n)
+    are = _lib.darr([complex(v).real for v in a])
+    aim = _lib.darr([complex(v).imag for v in a])
+    res = (ctypes.c_double * 16)()
+    _lib.check(_lib.load().gbf_axpy_norm2(out.layout.op, out.ptr, are, aim, x.ptr, y.ptr, x.nhalves(), res,
+                                          stream_ptr()))
+    r = [res[i] for i in range(n)]
+    return r[0] if n == 1 else r
+
+
+def inner_product_norm2(x, y):
+    """gpt.inner_product_norm2 (transform.py:121-131): (<x, y>, |x|^2)."""
+    return inner_product(x, y), norm2(x)
+
+
 def copy(dst, src):
     dst.tensor.copy_(src.tensor)
     return dst

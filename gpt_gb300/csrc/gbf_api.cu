@@ -778,6 +778,38 @@ int gbf_axpby(gbf_op* op, void* out, const double* a_re, const double* a_im, con
   });
 }
 
+int gbf_axpy_norm2(gbf_op* op, void* out, const double* a_re, const double* a_im, const void* x, const void* y,
+                   int nhalves, double* out_norm2, void* stream) {
+  return guarded([&] {
+    if (!op || !out || !x || !y || !a_re || !out_norm2) throw Fail(GBF_E_ARG, "null argument");
+    if (nhalves != 1 && nhalves != 2) throw Fail(GBF_E_ARG, "nhalves must be 1 or 2");
+    ensure_ws(op);
+    cudaStream_t s = (cudaStream_t)stream;
+    double acc[kMaxRhs] = {0};
+    for (int h = 0; h < nhalves; ++h) {
+      BlasArgs a{};
+      a.g = op->g;
+      a.out = (char*)out + h * op->half();
+      a.x = (const char*)x + h * op->half();
+      a.y = (const char*)y + h * op->half();
+      for (int r = 0; r < op->g.nrhs; ++r) {
+        a.a_re[r] = a_re[r];
+        a.a_im[r] = a_im ? a_im[r] : 0.0;
+        a.b_re[r] = 1.0;
+      }
+      a.write = 1;
+      a.red = 2;
+      a.ra = op->red(FIN_STORE);
+      CK(launch_blas(op->prec, a, s));
+      count_launch();
+      double r1[kMaxRhs];
+      read_last(op, s, r1, nullptr);
+      for (int r = 0; r < op->g.nrhs; ++r) acc[r] += r1[r];
+    }
+    for (int r = 0; r < op->g.nrhs; ++r) out_norm2[r] = acc[r];
+  });
+}
+
 int gbf_convert(gbf_op* dst_op, void* dst, gbf_op* src_op, const void* src, double scale, int nhalves, void* stream) {
   return guarded([&] {
     if (!dst_op || !src_op || !dst || !src) throw Fail(GBF_E_ARG, "null argument");

@@ -122,6 +122,11 @@ int gbf_inner(gbf_op* op, const void* x, const void* y, int nhalves, double* out
 /* out = a*x + b*y per rhs (a complex as a_re/a_im, b real; y may be NULL) */
 int gbf_axpby(gbf_op* op, void* out, const double* a_re, const double* a_im, const void* x, const double* b, const void* y,
               int nhalves, void* stream);
+/* out = a*x + y and |out|^2 per rhs in one pass (the fused form of
+ * lib/gpt/core/transform.py:139-153 axpy then norm2, the CG's axpy_norm2,
+ * cg.py:88); out may equal x or y. */
+int gbf_axpy_norm2(gbf_op* op, void* out, const double* a_re, const double* a_im, const void* x, const void* y,
+                   int nhalves, double* out_norm2, void* stream);
 /* dst = scale * src between two operators' layouts (same geometry), the
  * precision change of mixed-precision solvers (cgpt transform.cc:128-141). */
 int gbf_convert(gbf_op* dst_op, void* dst, gbf_op* src_op, const void* src, double scale, int nhalves, void* stream);

@@ -363,6 +363,38 @@ def test_reductions_bitwise_deterministic():
     assert n1 == n2
 
 
+@pytest.mark.parametrize("prec,tol", [(g.double, 1e-14), (g.double_float, 1e-13), (g.single, 1e-6)])
+def test_vector_algebra_matches_numpy(prec, tol):
+    """norm2, inner_product, axpy and the fused axpy_norm2 and
+    inner_product_norm2 (lib/gpt/core/transform.py:101-153) against numpy on
+    full fields, one and three packed right-hand sides."""
+    dims = [4, 4, 4, 8]
+    U = g.qcd.gauge.random_su3(g.grid(dims), 0.3, 8).U
+    V = int(np.prod(dims))
+    for nrhs in (1, 3):
+        op = gpu_op("wilson_clover", U, dims, g.double, **dict(WC, n_rhs=nrhs))
+        op = op if prec is g.double else op.converted(prec)
+        xs = [rand_field((V, 4, 3), 10 + k) for k in range(nrhs)]
+        ys = [rand_field((V, 4, 3), 20 + k) for k in range(nrhs)]
+        x, y = op.F_lattice(), op.F_lattice()
+        x[:] = xs[0] if nrhs == 1 else np.stack(xs)
+        y[:] = ys[0] if nrhs == 1 else np.stack(ys)
+        a = [0.3 - 0.7j, 1.5 + 0.2j, -0.4j][:nrhs]
+        d = op.F_lattice()
+        n2 = g.axpy_norm2(d, a if nrhs > 1 else a[0], x, y)
+        n2 = [n2] if nrhs == 1 else n2
+        got = d[:] if nrhs > 1 else [d[:]]
+        for k in range(nrhs):
+            want = a[k] * xs[k] + ys[k]
+            assert np.linalg.norm(got[k] - want) / np.linalg.norm(want) < tol
+            assert abs(n2[k] / np.vdot(want, want).real - 1) < tol
+        ip, nx = g.inner_product_norm2(x, y)
+        ip, nx = ([ip], [nx]) if nrhs == 1 else (ip, nx)
+        for k in range(nrhs):
+            assert abs(ip[k] - np.vdot(xs[k], ys[k])) / abs(np.vdot(xs[k], ys[k])) < tol
+            assert abs(nx[k] / np.vdot(xs[k], xs[k]).real - 1) < tol
+
+
 @pytest.mark.parametrize("kind,params", [("wilson_clover", WC), ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1))])
 def test_device_loop_equals_host_checked_graphs(kind, params):
     """The CG loop as host-checked graphs (the default 16 and 8 iterations),
