@@ -203,6 +203,27 @@ class fermion_operator(matrix_operator):
 
         return matrix_operator(prop)
 
+    def bulk_propagator(self, solver):
+        """Domain-wall operators (mobius.py:118-135): solver(op) * Import, the
+        5D solution; bulk_propagator_to_propagator (= Export) projects it to
+        the 4D propagator."""
+        if self.name not in ("mobius", "zmobius"):
+            raise NotImplementedError("bulk_propagator is defined for the domain-wall operators")
+        imp = self.ImportPhysicalFermionSource
+        inv_matrix = solver(self)
+
+        def prop(dst, src):
+            inv_matrix(dst, imp(src))
+
+        m = matrix_operator(prop)
+        m._new_dst = lambda src: self.F_lattice()
+        return m
+
+    @property
+    def bulk_propagator_to_propagator(self):
+        """mobius.py:69: the 4D solution P- psi_0 + P+ psi_{Ls-1} of a 5D field."""
+        return self.ExportPhysicalFermionSolution
+
     def even_odd_sites_decomposed(self, parity):
         return _even_odd_sites(self, parity)
 

@@ -129,3 +129,19 @@ def test_madwf_zmobius_inner_approximates_the_mobius_propagator():
     dc = qm.propagator(inv.defect_correcting(mdwf, eps=1e-6, maxiter=10))(S)[:]
     eps2 = np.linalg.norm(dc - exact) ** 2 / np.linalg.norm(exact) ** 2
     assert eps2 < 1e-10, eps2
+
+
+def test_bulk_propagator_projects_to_the_propagator():
+    """qm.bulk_propagator_to_propagator * qm.bulk_propagator(slv) ==
+    qm.propagator(slv) (tests/qcd/domain_wall.py:171-176)."""
+    U = _gauge()
+    qm = g.qcd.fermion.mobius(U, dict(MOBIUS, Ls=6))
+    slv = _solvers(1e-10)
+    src4 = _rand((int(np.prod(DIMS)), 4, 3), 8)
+    S = qm.U_lattice()
+    S[:] = src4
+    bulk = qm.bulk_propagator(slv)(S)
+    assert bulk.layout is qm.F_layout
+    via_bulk = qm.bulk_propagator_to_propagator(bulk)[:]
+    direct = qm.propagator(slv)(S)[:]
+    assert np.linalg.norm(via_bulk - direct) / np.linalg.norm(direct) < 1e-12
