@@ -28,8 +28,8 @@ class cg:
         # iterations_per_graph K > 0: CUDA graphs of K iterations with a host
         # convergence check between them; 0: the library's default K (16);
         # -1: the whole CG loop on the device (one CUDA graph with a
-        # conditional while node), for single-threaded use.  profile: no
-        # graphs, every kernel launched from the host between CUDA events
+        # conditional while node).  profile: no graphs, every kernel
+        # launched from the host between CUDA events
         self.iterations_per_graph = p.get("iterations_per_graph", iterations_per_graph)
         self.profile = bool(p.get("profile", profile))
         self.history = []

@@ -293,6 +293,20 @@ void setup_geo(gbf_op* op) {
   op->g4.fLs = FastDiv(1u);
 }
 
+// Host -> device copy that has completed when it returns, on a stream of its
+// own (a plain cudaMemcpy from pageable memory may still be in flight on the
+// legacy default stream, which the operators' non-blocking streams do not
+// wait for)
+void upload(void* dst, const void* src, size_t bytes) {
+  cudaStream_t t;
+  CK(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking));
+  const cudaError_t e1 = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, t);
+  const cudaError_t e2 = cudaStreamSynchronize(t);
+  cudaStreamDestroy(t);
+  CK(e1);
+  CK(e2);
+}
+
 // Cayley s-matrices of the Mobius / zmobius operator with per-slice b_s, c_s
 // (mobius: b, c for every s, lib/gpt/qcd/fermion/mobius.py:29-46; zmobius:
 // b_s = ((b + c) / omega_s + (b - c)) / 2, c_s = ((b + c) / omega_s - (b - c)) / 2,
@@ -391,7 +405,7 @@ void build_smat(gbf_op* op) {
   const size_t bytes = all.size() * 2 * op->rb();  // room for the complex layout
   if (!op->smat) op->smat = dmalloc(bytes);
   if (op->prec == P64) {
-    CK(cudaMemcpy(op->smat, flat.data(), flat.size() * 8, cudaMemcpyHostToDevice));
+    upload(op->smat, flat.data(), flat.size() * 8);
   } else if (op->prec == PDD) {
     std::vector<float> f(2 * flat.size());
     for (size_t i = 0; i < flat.size(); ++i) {
@@ -399,10 +413,10 @@ void build_smat(gbf_op* op) {
       f[2 * i] = v.h;
       f[2 * i + 1] = v.l;
     }
-    CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+    upload(op->smat, f.data(), f.size() * 4);
   } else {
     std::vector<float> f(flat.begin(), flat.end());
-    CK(cudaMemcpy(op->smat, f.data(), f.size() * 4, cudaMemcpyHostToDevice));
+    upload(op->smat, f.data(), f.size() * 4);
   }
 }
 
@@ -416,11 +430,16 @@ void ensure_ws(gbf_op* op) {
   op->partial = (double2*)dmalloc((size_t)maxblocks * op->g.nrhs * sizeof(double2));
   op->partial_cap = maxblocks * op->g.nrhs;
   op->counter = (unsigned*)dmalloc(sizeof(unsigned) * 4);
-  CK(cudaMemset(op->counter, 0, sizeof(unsigned) * 4));
   op->st = (CGState*)dmalloc(sizeof(CGState));
-  CK(cudaMemset(op->st, 0, sizeof(CGState)));
   CK(cudaMallocHost(&op->hst, 2 * sizeof(CGState)));
   CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  // zero the counter and the CG state on the op's own stream and wait: a
+  // cudaMemset would go to the legacy default stream, which non-blocking
+  // streams do not wait for, so it could land after this op's first kernels
+  // (seen as CG states reset between cg_init and the loop)
+  CK(cudaMemsetAsync(op->counter, 0, sizeof(unsigned) * 4, op->stream));
+  CK(cudaMemsetAsync(op->st, 0, sizeof(CGState), op->stream));
+  CK(cudaStreamSynchronize(op->stream));
   CK(cudaEventCreateWithFlags(&op->ev_in, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&op->ev_out, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&op->ev_chk[0], cudaEventDisableTiming));
@@ -1075,7 +1094,8 @@ bool cg_loop(gbf_op* op, cudaStream_t s, const gbf_cg_params* prm, double* kms, 
       kcount[0] += 4;
       kcount[1] += 1;
       kcount[2] += 1;
-      CK(cudaMemcpy(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpyAsync(op->hst, op->st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
       if (op->hst->all_done) break;
     }
     for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);

@@ -144,10 +144,7 @@ typedef struct {
                                checks convergence between graph launches (kernels of iterations
                                past convergence return at once); 0: K = 16; -1: the whole loop
                                on the device, one CUDA graph with a conditional while node and no
-                               host round trip.  Bitwise equal solutions in all modes.  With -1,
-                               2 of 160 solves that ran concurrently with solves of other
-                               operators on other host threads returned after zero iterations
-                               (reported as not converged); use it from one thread only. */
+                               host round trip.  Bitwise equal solutions in all modes. */
   int profile;              /* 1: no graphs; CUDA events time every kernel class (diagnostic run) */
 } gbf_cg_params;
 typedef struct {
