@@ -237,6 +237,11 @@ def run_mobius_config(args, which):
     clk = clocks.stop()
     total_ms = e0.elapsed_time(e1)
     inner_its = (inner_cg.total_iterations - before) // max(1, args.steps)
+    # device memory in use with the operators, Krylov workspace and the last
+    # group's fields resident (every allocation on the GPU, torch's and the
+    # library's, as total - free)
+    free_b, total_b = torch.cuda.mem_get_info()
+    used_gb = (total_b - free_b) / 1e9
     # true residual of the 5D systems of the last step, FP64
     worst = 0.0
     for b5, x5 in last5.values():  # the last group solved
@@ -292,7 +297,8 @@ def run_mobius_config(args, which):
     line = _common_line(METRIC, value, "solves/s", args, 1, total_ms, cfg, f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",
                         {"gpu_launches": int(n1 - n0), "clocks": clk, "true_residual_5d": worst,
                          "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
-                         "ms_per_solve": total_ms / args.steps / nsrc, **plain,
+                         "ms_per_solve": total_ms / args.steps / nsrc,
+                         "device_memory_used_gb": used_gb, "device_memory_total_gb": total_b / 1e9, **plain,
                          **({"rhs_group_tuning": rhs_tuning["results"]} if rhs_tuning else {})})
     print(json.dumps(line), flush=True)
     return 0
