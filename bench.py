@@ -22,6 +22,7 @@ bounded sample of inner CG iterations and outer residuals, scaled to solves/s
 with the iteration counts of one full CPU solve done during warm-up.
 """
 import argparse
+import gc
 import json
 import math
 import os
@@ -176,6 +177,7 @@ def run_mobius_config(args, which):
             lambda k: g.qcd.fermion.mobius_operator(U, dict(base, n_rhs=k), precision=inner_prec), nsrc,
             candidates=cands, budget_bytes=int(0.85 * free))
         group = rhs_tuning["params"][0]
+        gc.collect()
         torch.cuda.empty_cache()
     inner_tol = 1e-5 if args.inner == "single" else 3e-3
     V = grid.gsites
@@ -238,10 +240,14 @@ def run_mobius_config(args, which):
     total_ms = e0.elapsed_time(e1)
     inner_its = (inner_cg.total_iterations - before) // max(1, args.steps)
     # device memory in use with the operators, Krylov workspace and the last
-    # group's fields resident (every allocation on the GPU, torch's and the
-    # library's, as total - free)
+    # group's fields resident: every live allocation on the GPU, torch's and
+    # the library's, as total - free after torch's cache of freed blocks is
+    # released; beside it the peak of torch's live tensors
+    gc.collect()
+    torch.cuda.empty_cache()
     free_b, total_b = torch.cuda.mem_get_info()
     used_gb = (total_b - free_b) / 1e9
+    torch_peak_gb = torch.cuda.max_memory_allocated() / 1e9
     # true residual of the 5D systems of the last step, FP64
     worst = 0.0
     for b5, x5 in last5.values():  # the last group solved
@@ -298,7 +304,8 @@ def run_mobius_config(args, which):
                         {"gpu_launches": int(n1 - n0), "clocks": clk, "true_residual_5d": worst,
                          "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
                          "ms_per_solve": total_ms / args.steps / nsrc,
-                         "device_memory_used_gb": used_gb, "device_memory_total_gb": total_b / 1e9, **plain,
+                         "device_memory_used_gb": used_gb, "device_memory_total_gb": total_b / 1e9,
+                         "torch_peak_allocated_gb": torch_peak_gb, **plain,
                          **({"rhs_group_tuning": rhs_tuning["results"]} if rhs_tuning else {})})
     print(json.dumps(line), flush=True)
     return 0

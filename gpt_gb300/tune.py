@@ -12,6 +12,7 @@ The cache directory is $GPT_GB300_TUNE_DIR, default ".gpt_gb300_tune" in
 the working directory.
 """
 import ctypes
+import gc
 import hashlib
 import json
 import os
@@ -144,6 +145,10 @@ def rhs_group(make_op, n_sources, candidates=None, budget_bytes=None, iterations
         if per_rhs is None:
             per_rhs = max(1, used)
         del op, b, x
+        # an operator object is part of reference cycles (its matrix
+        # operators close over it): collect it now so that its device memory
+        # is released before the next, larger candidate
+        gc.collect()
         torch.cuda.synchronize()
     best = min(results, key=lambda kr: math.ceil(n_sources / kr[0]) * kr[1])
     data = {"tag": tag, "params": [int(best[0])], "results": [[int(k), float(ms)] for k, ms in results]}
