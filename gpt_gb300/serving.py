@@ -23,6 +23,7 @@ fixed summation order and no request shares buffers with another.
 """
 import collections
 import dataclasses
+import gc
 import math
 import threading
 import time
@@ -223,6 +224,15 @@ def gpu_executor(keep_solution=False, inner_tol=1e-5, iterations_per_graph=0):
     from .qcd import fermion, gauge
 
     def run(req, method):
+        try:
+            return _run(req, method)
+        finally:
+            # operator objects sit in reference cycles (their matrix operators
+            # close over them): collect them now so that the request's device
+            # memory returns before the admission of the next one
+            gc.collect()
+
+    def _run(req, method):
         stream = torch.cuda.Stream()
         with torch.cuda.stream(stream):
             grid = core.grid([req.L] * 4, core.double)
