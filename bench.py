@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--dims", type=str, default=None, help="override lattice, e.g. 16,16,16,16 (tests only)")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-next-rows", action="store_true",
+                    help="c2: skip the measurements of the rows beyond the hot path after the timed region")
     ap.add_argument("--no-dhop-benchmark", action="store_true",
                     help="c2: skip the reference's Dslash benchmark (Mobius Dhop 64.32.32.32 Ls 12) after the timed region")
     ap.add_argument("--profile-dslash", action="store_true",
@@ -518,11 +520,23 @@ def run_profile_next(args):
 
 
 def run_next_rows(args):
-    """--config next: one measurement per row beyond the hot path, on
-    synthetic inputs (gauge exp(i eps H), Gaussian sources), CUDA-event
-    timing after warm-up.  Algorithmic bytes count every field once per
-    kernel (the hop: input spinor, 8 links, output, plus X and the site-local
-    terms), as for the main roofline figure."""
+    """--config next: the measurements of next_rows_measurements() as one line."""
+    t0 = time.time()
+    out = next_rows_measurements()
+    line = {"metric": "rows beyond the hot path: kernel GB/s, solver speed-ups, IO MB/s", "value": None,
+            "unit": None, "n_gpus": 1, "data": "synthetic", "config": {"workload": "see each entry"},
+            "block_cg": "measured by --config c3 --solver block_cg", "seconds": time.time() - t0}
+    line.update(out)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def next_rows_measurements():
+    """One measurement per row beyond the hot path, on synthetic inputs
+    (gauge exp(i eps H), Gaussian sources), CUDA-event timing after warm-up.
+    Algorithmic bytes count every field once per kernel (the hop: input
+    spinor, 8 links, output, plus X and the site-local terms), as for the
+    main roofline figure."""
     import tempfile
 
     import torch
@@ -674,12 +688,8 @@ def run_next_rows(args):
             os.remove(fn)
     out["gauge_io_32^4_fp64"] = res
 
-    line = {"metric": "rows beyond the hot path: kernel GB/s, solver speed-ups, IO MB/s", "value": None,
-            "unit": None, "n_gpus": 1, "data": "synthetic", "config": {"workload": "see each entry"},
-            "block_cg": "measured by --config c3 --solver block_cg", "seconds": time.time() - t_all}
-    line.update(out)
-    print(json.dumps(line), flush=True)
-    return 0
+    out["seconds"] = time.time() - t_all
+    return out
 
 
 def run_c5(args):
@@ -1112,9 +1122,17 @@ def run_gbf(args, dims):
         del op_o
 
     # ---- the reference's own Dslash benchmark (benchmarks/dslash.py), after the timed region ----
-    dhop = None
+    dhop = nxt = None
     if world == 1 and not args.no_dhop_benchmark:
-        dhop = dwf_dhop_benchmark()
+        try:
+            dhop = dwf_dhop_benchmark()
+        except Exception as e:  # reported, not fatal for the headline line
+            dhop = {"error": f"{type(e).__name__}: {e}"}
+    if world == 1 and not args.no_next_rows:
+        try:
+            nxt = next_rows_measurements()
+        except Exception as e:
+            nxt = {"error": f"{type(e).__name__}: {e}"}
 
     p = sorted(step_ms)
     line = {
@@ -1165,6 +1183,7 @@ def run_gbf(args, dims):
                                    "true_residual_fp64": mixed_dd_true},
         },
         "reference_dslash_benchmark": dhop,
+        "rows_beyond_the_hot_path": nxt,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
