@@ -542,7 +542,7 @@ def next_rows_measurements():
     import torch
 
     import gpt_gb300 as g
-    from gpt_gb300 import _lib, core
+    from gpt_gb300 import core
 
     L = g.load()
     stream = torch.cuda.current_stream()
@@ -719,8 +719,7 @@ def run_c5(args):
     n1 = L.gbf_launch_count()
     s = serving.summarize(res, wall)
     serial, swall = serving.Server(ex, budget, caps={8: 1, 16: 1, 24: 1, 32: 1}, method="plain", realtime=False).run(reqs)
-    for r in serial:  # serial: one request at a time, so latency = completion - arrival of a queue drained in order
-        pass
+    # serial: one request per lattice size at a time, drained in arrival order
     ss = serving.summarize(serial, swall)
     cfg = {"workload": f"serving: {args.requests} Poisson requests at 20/s, wilson_clover L^4 L in {{8,16,24,32}}, "
                        "gauge eps U[0.2,0.5], mass U[0.01,0.2], 1-12 gaussian sources, true residual 1e-10; "

@@ -215,8 +215,6 @@ def gpu_executor(keep_solution=False, inner_tol=1e-5, iterations_per_graph=0):
     fresh device-generated gauge field; mixed = defect_correcting(
     mixed_precision(preconditioned(eo2_ne, cg(inner_tol))), single, double);
     plain = preconditioned(eo2_ne, cg(tol / 3)) in FP64."""
-    import ctypes
-
     import torch
 
     from . import _lib, core
