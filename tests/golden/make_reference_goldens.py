@@ -12,6 +12,9 @@ are extracted -- no code -- from:
   tests/qcd/fermion_operators.py:338-524 Grid operator fingerprints (wilson,
                                          wilson_clover, wilson_twisted_mass,
                                          mobius, mobius_axial_mass, zmobius)
+  tests/qcd/fermion_operators.py:193-218 Wilson point-source correlator
+  tests/qcd/domain_wall.py:193-209       Mobius J5q correlator
+  tests/qcd/domain_wall.py:248-274       Mobius point-source correlator
 """
 import ast
 import json
@@ -124,6 +127,25 @@ out["fingerprints"] = {
     "wilson_clover": {"params": params["wilson_clover_params"], "matrices": mats["wilson_clover_matrices"]},
     "wilson_twisted_mass": {"params": params["wilson_twisted_mass_params"], "matrices": mats["wilson_twisted_mass_matrices"]},
     **mob,
+}
+# solve-level goldens: correlators of point-source propagators (single precision in the reference)
+out["wilson_correlator"] = {
+    "cite": "tests/qcd/fermion_operators.py:12-34 (gauge, parameters), 137-158 (point source, eo2_ne cg), "
+            "190-218 (correlator)",
+    "seed": "test", "grid": [8, 8, 8, 16], "gauge_scale": 1.0, "single": True, "kappa": 0.137,
+    "boundary_phases_exp_i": [1, 2, 3, 4], "point": [1, 0, 0, 0], "cg_eps": 1e-6,
+    "correlator": num(lit(fo, "correlator_ref")), "tol": 1e-5,
+}
+dw = read("tests/qcd/domain_wall.py")
+mp = lit(dw, "mobius_params")
+mp = {ast.literal_eval(k): num(v) for k, v in zip(mp.keys, mp.values)}
+out["mobius_correlators"] = {
+    "cite": "tests/qcd/domain_wall.py:15-33 (gauge, parameters), 117-127 (point source, eo2_ne cg), "
+            "171-177 (bulk propagator), 193-209 (J5q), 248-274 (correlator)",
+    "seed": "test", "grid": [8, 8, 8, 8], "gauge_scale": 2.0, "single": True, "params": mp,
+    "point": [0, 1, 0, 0], "cg_eps": 1e-5,
+    "J5q": num(lit(dw, "J5q_ref")), "J5q_tol": 1e-5,
+    "correlator": num(lit(dw, "correlator_ref")), "correlator_tol": 1e-5,
 }
 with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json"), "w") as f:
     json.dump(out, f, indent=1)

@@ -181,3 +181,75 @@ def test_oracle_solvers_true_residual():
     x2, it2, nout, tres = op.defect_correcting(src, 1e-10, 20, 1e-5, 1000)
     assert tres < 1e-10
     assert np.sqrt(o.norm2(x - x2) / o.norm2(x)) < 1e-8
+
+
+# ---------------------------------------------------------------------------
+# solve-level goldens: point-source propagators of the RNG's gauge fields
+# (single precision links, as in the reference), contracted to correlators
+# ---------------------------------------------------------------------------
+def _point_propagator_correlator(solve_column, V, point_index, n_t, per_slice):
+    corr = np.zeros(n_t)
+    extra = []
+    for col in range(12):
+        src = np.zeros((V, 4, 3), dtype=np.complex128)
+        src[point_index, col // 3, col % 3] = 1.0
+        x4, aux = solve_column(src)
+        corr += (np.abs(x4.reshape(n_t, per_slice, 12)) ** 2).sum(axis=(1, 2))
+        extra.append(aux)
+    return corr, extra
+
+
+def test_wilson_point_correlator_golden():
+    """tests/qcd/fermion_operators.py:190-218: the eo2_ne propagator of a
+    point source on g.qcd.gauge.random(rng "test") links in single precision,
+    kappa 0.137, boundary phases exp(i k), contracted to
+    sum_x tr(D(x) D(x)^+) per time slice, within the reference's 1e-5."""
+    G = GOLD["wilson_correlator"]
+    dims = G["grid"]
+    g = o.grid(dims)
+    U = o.random(G["seed"]).gauge(g, G["gauge_scale"]).astype(np.complex64).astype(np.complex128)
+    ph = [complex(np.cos(k), np.sin(k)) for k in G["boundary_phases_exp_i"]]
+    w = o.wilson_clover(U, dims, kappa=G["kappa"], boundary_phases=ph)
+    p = G["point"]
+    idx = p[0] + dims[0] * (p[1] + dims[1] * (p[2] + dims[2] * p[3]))
+
+    def solve(src):
+        x, it, res = w.eo2ne_cg(src, 1e-8, 5000)
+        return x, it
+
+    corr, its = _point_propagator_correlator(solve, g.V, idx, dims[3], g.V // dims[3])
+    assert np.linalg.norm(corr - np.array(G["correlator"])) < G["tol"]
+
+
+def test_mobius_point_correlator_and_J5q_goldens():
+    """tests/qcd/domain_wall.py:171-274: Mobius (Ls 12, b 1.5, c 0.5, M5 1.8,
+    mass 0.08) propagator of a point source, Import -> eo2_ne CG -> Export,
+    on g.qcd.gauge.random(rng "test", scale 2) links in single precision:
+    the correlator sum_x tr(D D^+) per time slice (eps_qm < 1e-5) and the
+    midpoint density J5q = P+ psi_{Ls/2-1} + P- psi_{Ls/2} of the 5D
+    solution (mobius.py:55-61) contracted the same way (within 1e-5)."""
+    G = GOLD["mobius_correlators"]
+    dims = G["grid"]
+    g = o.grid(dims)
+    U = o.random(G["seed"]).gauge(g, G["gauge_scale"]).astype(np.complex64).astype(np.complex128)
+    prm = G["params"]
+    Ls = int(prm["Ls"])
+    qm = o.mobius(U, dims, Ls=Ls, b=prm["b"], c=prm["c"], M5=prm["M5"], mass=prm["mass"],
+                  boundary_phases=prm["boundary_phases"])
+    p = G["point"]
+    idx = p[0] + dims[0] * (p[1] + dims[1] * (p[2] + dims[2] * p[3]))
+    n_t, per = dims[3], g.V // dims[3]
+    j5 = np.zeros(n_t)
+
+    def solve(src):
+        x5, it, res = qm.eo2ne_cg(qm.import_physical_source(src), 1e-7, 20000)
+        mid = np.concatenate([x5[:, Ls // 2 - 1, 0:2], x5[:, Ls // 2, 2:4]], axis=1)  # [V, 4, 3]
+        return qm.export_physical_solution(x5), mid
+
+    corr, mids = _point_propagator_correlator(solve, g.V, idx, n_t, per)
+    for mid in mids:
+        j5 += (np.abs(mid.reshape(n_t, per, 12)) ** 2).sum(axis=(1, 2))
+    assert np.linalg.norm(corr - np.array(G["correlator"])) / len(corr) < G["correlator_tol"]
+    assert np.linalg.norm(j5 - np.array(G["J5q"])) < G["J5q_tol"]
+    # the J5q values are O(1e-5): check them relatively as well
+    assert np.abs(j5 / np.array(G["J5q"]) - 1).max() < 1e-3
