@@ -14,7 +14,9 @@ are extracted -- no code -- from:
                                          mobius, mobius_axial_mass, zmobius)
   tests/qcd/fermion_operators.py:193-218 Wilson point-source correlator
   tests/qcd/domain_wall.py:193-209       Mobius J5q correlator
-  tests/qcd/domain_wall.py:248-274       Mobius point-source correlator
+  tests/qcd/domain_wall.py:248-274       Mobius point-source correlator, and
+                                         the zmobius (domain_wall.py:91-112)
+                                         propagator's correlator against it
 """
 import ast
 import json
@@ -139,6 +141,17 @@ out["wilson_correlator"] = {
 dw = read("tests/qcd/domain_wall.py")
 mp = lit(dw, "mobius_params")
 mp = {ast.literal_eval(k): num(v) for k, v in zip(mp.keys, mp.values)}
+def call_dict(src, name):
+    """The literal params dict passed to the call assigned to `name`."""
+    for node in ast.walk(ast.parse(src)):
+        if isinstance(node, ast.Assign) and any(isinstance(t, ast.Name) and t.id == name for t in node.targets):
+            d = node.value.args[1]
+            return {ast.literal_eval(k): num(v) for k, v in zip(d.keys, d.values)}
+    raise KeyError(name)
+
+
+zp = call_dict(dw, "qz")
+zp["omega"] = [[complex(w).real, complex(w).imag] for w in zp["omega"]]
 out["mobius_correlators"] = {
     "cite": "tests/qcd/domain_wall.py:15-33 (gauge, parameters), 117-127 (point source, eo2_ne cg), "
             "171-177 (bulk propagator), 193-209 (J5q), 248-274 (correlator)",
@@ -146,6 +159,7 @@ out["mobius_correlators"] = {
     "point": [0, 1, 0, 0], "cg_eps": 1e-5,
     "J5q": num(lit(dw, "J5q_ref")), "J5q_tol": 1e-5,
     "correlator": num(lit(dw, "correlator_ref")), "correlator_tol": 1e-5,
+    "zmobius_params": zp, "zmobius_correlator_tol": 5e-4,
 }
 with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json"), "w") as f:
     json.dump(out, f, indent=1)

@@ -227,7 +227,9 @@ def test_mobius_point_correlator_and_J5q_goldens():
     on g.qcd.gauge.random(rng "test", scale 2) links in single precision:
     the correlator sum_x tr(D D^+) per time slice (eps_qm < 1e-5) and the
     midpoint density J5q = P+ psi_{Ls/2-1} + P- psi_{Ls/2} of the 5D
-    solution (mobius.py:55-61) contracted the same way (within 1e-5)."""
+    solution (mobius.py:55-61) contracted the same way (within 1e-5); and
+    the correlator of the zmobius operator of domain_wall.py:91-112 against
+    the same golden (eps_qz < 5e-4)."""
     G = GOLD["mobius_correlators"]
     dims = G["grid"]
     g = o.grid(dims)
@@ -253,3 +255,15 @@ def test_mobius_point_correlator_and_J5q_goldens():
     assert np.linalg.norm(j5 - np.array(G["J5q"])) < G["J5q_tol"]
     # the J5q values are O(1e-5): check them relatively as well
     assert np.abs(j5 / np.array(G["J5q"]) - 1).max() < 1e-3
+    # zmobius (Ls 10, complex omega) approximating this Mobius operator: its
+    # correlator against the same golden, the reference's eps_qz < 5e-4
+    zp = G["zmobius_params"]
+    qz = o.zmobius(U, dims, omega=zp["omega"], b=zp["b"], c=zp["c"], M5=zp["M5"], mass=zp["mass"],
+                   boundary_phases=zp["boundary_phases"])
+
+    def solve_z(src):
+        x5, it, res = qz.eo2ne_cg(qz.import_physical_source(src), 1e-6, 20000)
+        return qz.export_physical_solution(x5), it
+
+    corr_z, _ = _point_propagator_correlator(solve_z, g.V, idx, n_t, per)
+    assert np.linalg.norm(corr_z - np.array(G["correlator"])) / len(corr_z) < G["zmobius_correlator_tol"]
