@@ -219,6 +219,21 @@ class fermion_operator(matrix_operator):
         m._new_dst = lambda src: self.F_lattice()
         return m
 
+    def J5q(self, src5):
+        """The midpoint density of a domain-wall field (mobius.py:55-61):
+        dst4 = P+ psi_{Ls/2-1} + P- psi_{Ls/2}, as the chiral shift P^+
+        (slice s gets P- psi_s + P+ psi_{s-1}) followed by a copy of slice
+        Ls/2 into a 4D field."""
+        if self.name not in ("mobius", "zmobius"):
+            raise NotImplementedError("J5q is defined for the domain-wall operators")
+        L = _lib.load()
+        y = self.F_lattice()
+        _lib.check(L.gbf_chiral_shift(src5.layout.op, src5.ptr, y.ptr, -1, 2, core.stream_ptr()))
+        dst = self.U_lattice()
+        _lib.check(L.gbf_copy_slices(dst.layout.op, dst.ptr, 0, y.layout.op, y.ptr, self.Ls // 2, 1, 1.0, 2,
+                                     core.stream_ptr()))
+        return dst
+
     @property
     def bulk_propagator_to_propagator(self):
         """mobius.py:69: the 4D solution P- psi_0 + P+ psi_{Ls-1} of a 5D field."""

@@ -145,3 +145,14 @@ def test_bulk_propagator_projects_to_the_propagator():
     via_bulk = qm.bulk_propagator_to_propagator(bulk)[:]
     direct = qm.propagator(slv)(S)[:]
     assert np.linalg.norm(via_bulk - direct) / np.linalg.norm(direct) < 1e-12
+
+
+def test_J5q_matches_numpy_midpoint():
+    """qm.J5q(psi) = P+ psi_{Ls/2-1} + P- psi_{Ls/2} (mobius.py:55-61) on a
+    random 5D field, against numpy on the natural layout."""
+    U = _gauge()
+    qm = g.qcd.fermion.mobius(U, dict(MOBIUS, Ls=6))
+    x = _rand(qm.F_lattice()[:].shape, 9)  # [V, Ls, 4, 3]
+    got = qm.J5q(_field(qm, x))[:]
+    want = np.concatenate([x[:, 2, 0:2], x[:, 3, 2:4]], axis=1)
+    assert np.array_equal(got, want)
