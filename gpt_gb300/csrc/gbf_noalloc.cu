@@ -11,11 +11,16 @@
 // Limits and rules (also stated in include/gbferm.h):
 //   * at most kNoAllocMaxSites 5D sites per checkerboard half (16384 blocks
 //     of 256 sites); larger fields are rejected with GBF_E_ARG;
-//   * the array (about 263 KB) is reserved on every GPU that loads the
-//     library, for the life of the process;
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture;
+//   * the array (about 263 KB) is held on every GPU where the library's
+//     module is loaded, for the life of the process.  CUDA loads modules
+//     lazily (the default since CUDA 12.2), so the module holding this array
+//     and its kernels is loaded, and the array's memory taken, on the first
+//     call on a device, when cudaGetSymbolAddress looks up the array's
+//     device address (once per device, with that device current);
+//   * so make that first call early: before any stream capture, and before
+//     a memory pool of the caller takes the device's free HBM (otherwise the
+//     module load itself can fail with out-of-memory).  A call with
+//     n_sites = 0 does only this set-up and launches nothing;
 //   * every call shares the one array: calls whose kernels overlap on the GPU
 //     (different streams, or concurrent host threads) race and give wrong sums.
 //     The block counter is cleared at the start of each call.

@@ -52,7 +52,8 @@ enum {
   GBF_M = 2001, GBF_MDAG = 2002, GBF_MEOOE = 2003, GBF_MEOOE_DAG = 2004,
   GBF_MOOEE = 2005, GBF_MOOEE_DAG = 2006, GBF_MOOEE_INV = 2007, GBF_MOOEE_INV_DAG = 2008,
   GBF_MDIAG = 2009, GBF_DMINUS = 2010, GBF_DMINUS_DAG = 2011,
-  GBF_IMPORT_PHYSICAL_FERMION_SOURCE = 2012, GBF_EXPORT_PHYSICAL_FERMION_SOLUTION = 2014,
+  GBF_IMPORT_PHYSICAL_FERMION_SOURCE = 2012, GBF_IMPORT_UNPHYSICAL_FERMION = 2013,
+  GBF_EXPORT_PHYSICAL_FERMION_SOLUTION = 2014, GBF_EXPORT_PHYSICAL_FERMION_SOURCE = 2015,
   GBF_DHOP = 3001, GBF_DHOP_EO = 3002, GBF_DHOP_DAG = 4001, GBF_DHOP_EO_DAG = 4002
 };
 
@@ -91,7 +92,11 @@ int gbf_update_gauge(gbf_op* op, const void* U, int on_device, void* stream);
  * geometry or clover parameters differ. */
 int gbf_update_gauge_from(gbf_op* op, const void* U, int on_device, const gbf_op* clover_from, void* stream);
 
-/* cgpt set_mass_fermion_operator (operators.cc:74-83). */
+/* cgpt set_mass_fermion_operator (operators.cc:74-83; the per-action
+ * semantics of lib/cgpt/lib/operators/implementation.h:21-45).  Mobius /
+ * zmobius: the two wall masses.  Wilson-clover and twisted mass: mass_plus is
+ * the new mass m (mass_minus is ignored); the diagonal term follows and a
+ * clover operator's clover term and inverse are updated on the device. */
 int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus);
 
 /* cgpt delete_fermion_operator (operators.cc:85-94). */
@@ -270,12 +275,15 @@ int gbf_random_spinor(long long n_complex, unsigned long long seed, void* out, v
  * use).  x: device field of `precision` with n_sites 5D sites per half and
  * nhalves halves (the layout of gbf_field_bytes); the sum over all sites is
  * written to the host double *out after the stream is synchronised.
- * The reduction scratch is a static device array of about 263 KB, reserved on
- * every GPU that loads the library until the process exits; at most
- * 4194304 sites per half (larger sizes return GBF_E_ARG).  The first call on
- * a device sets the array's address up for that device (make it before any
- * stream capture).  All calls share the array: calls that overlap on the GPU
- * race.  Errors: gbf_norm2_noalloc_error(). */
+ * The reduction scratch is a static device array of about 263 KB, held on
+ * every GPU where it is loaded until the process exits; at most 4194304
+ * sites per half (larger sizes return GBF_E_ARG).  CUDA loads the library's
+ * modules lazily, so the first call on a device loads this one (taking the
+ * array's memory) and looks up the array's address for that device: make
+ * that first call before any stream capture and before the caller's own pool
+ * takes the free HBM; a call with n_sites = 0 does only this set-up.  All
+ * calls share the array: calls that overlap on the GPU race.  Errors:
+ * gbf_norm2_noalloc_error(). */
 int gbf_norm2_noalloc(int precision, const void* x, long long n_sites, int nhalves, double* out, void* stream);
 const char* gbf_norm2_noalloc_error(void);
 

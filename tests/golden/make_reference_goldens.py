@@ -1,9 +1,9 @@
 """Extract the reference's own golden values for the fermion hot path into
 reference_goldens.json.
 
-Run in a container where the lehner/gpt sources are mounted (the default
-location is /root/reference; pass another root as argv[1]).  Only numbers
-are extracted -- no code -- from:
+Run where the lehner/gpt sources are mounted, giving their root as argv[1]
+or in the environment variable GPT_REFERENCE_ROOT.  Only numbers are
+extracted -- no code -- from:
 
   tests/core/checksums.py:11-21          sha256 of a test string (vs hashlib)
   tests/random/simple.py:17-31           plaquettes of g.qcd.gauge.random
@@ -24,7 +24,9 @@ import os
 import re
 import sys
 
-root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GPT_REFERENCE_ROOT")
+if not root:
+    sys.exit("usage: make_reference_goldens.py <root of the lehner/gpt sources> (or set GPT_REFERENCE_ROOT)")
 
 
 def read(p):
