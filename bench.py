@@ -17,9 +17,14 @@ FP64 eo2_ne CG (eps 1e-10) is measured beside it.  Inputs (gauge field
 no L2 flush is needed between steps.
 
 --impl reference runs the CPU restatement of the same solve (the reference's
-Grid CPU operator cannot be built here) on all host cores: each step is a
-bounded sample of inner CG iterations and outer residuals, scaled to solves/s
-with the iteration counts of one full CPU solve done during warm-up.
+Grid CPU operator cannot be built here) on all host cores: each step is one
+full mixed solve, timed.
+
+After the timed region the default line also carries compact measurements
+of the other configurations (c1, c3, c4, c5, each with the FP64 oracle
+residual of its solves), the reference's own Dslash benchmark and the rows
+beyond the hot path; the figures to read (mixed, plain, their ratio) come
+last in the line.
 """
 import argparse
 import gc
@@ -53,6 +58,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-next-rows", action="store_true",
                     help="c2: skip the measurements of the rows beyond the hot path after the timed region")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="c2: skip the compact c1, c3, c4 and c5 measurements after the timed region")
     ap.add_argument("--no-dhop-benchmark", action="store_true",
                     help="c2: skip the reference's Dslash benchmark (Mobius Dhop 64.32.32.32 Ls 12) after the timed region")
     ap.add_argument("--profile-dslash", action="store_true",
@@ -143,12 +150,16 @@ def _common_line(metric, value, unit, args, world, total_ms, dims_cfg, dtype, ex
     return line
 
 
-def run_mobius_config(args, which):
+def measure_mobius(which, warmup, steps, inner="single", solver_kind="cg", rhs_group=0, with_plain=False,
+                   max_groups=None, oracle_residual=True):
     """c3: Mobius 16^3x32, Ls 12, b 1.5, c 0.5, M5 1.8, mass 0.01, gauge eps 0.4,
     12 point sources (every spin-colour component at site 0) as one packed
     12-rhs field, propagator = Export * solve * Import, to true residual 1e-8.
     c4: Mobius 32^3x64, Ls 16, mass 0.005, 12 Gaussian sources, to 1e-10,
-    solved in groups of right-hand sides that fit HBM."""
+    solved in groups of right-hand sides that fit HBM (max_groups limits how
+    many groups one step solves).  With oracle_residual the FP64 oracle's
+    true residual |b - M x| / |b| of every 5D system of the last step is
+    computed on the host.  Returns (summary dict, total ms, config dict)."""
     import torch
 
     import gpt_gb300 as g
@@ -159,10 +170,10 @@ def run_mobius_config(args, which):
         group = 12
     else:
         dims, Ls, mass, geps, tol, nsrc = [32, 32, 32, 64], 16, 0.005, 0.4, 1e-10, 12
-        group = args.rhs_group
+        group = rhs_group
     grid = g.grid(dims, g.double)
     U = g.qcd.gauge.random_su3_device(grid, geps, 4242)
-    inner_prec = g.half if args.inner == "half" else g.single
+    inner_prec = g.half if inner == "half" else g.single
     rhs_tuning = None
     if not group:
         # RHS block size by the autotuner: time 3 inner CG iterations of the
@@ -181,14 +192,17 @@ def run_mobius_config(args, which):
         group = rhs_tuning["params"][0]
         gc.collect()
         torch.cuda.empty_cache()
-    inner_tol = 1e-5 if args.inner == "single" else 3e-3
+    inner_tol = 1e-5 if inner == "single" else 3e-3
     V = grid.gsites
     ngroups = (nsrc + group - 1) // group
+    if max_groups:
+        ngroups = min(ngroups, max_groups)
+    nsolved = min(nsrc, ngroups * group)
     params = dict(Ls=Ls, b=1.5, c=0.5, M5=1.8, mass=mass, boundary_phases=[1.0, 1.0, 1.0, -1.0], n_rhs=group)
     op = g.qcd.fermion.mobius(U, params)
     inv = g.algorithms.inverter
     pc = g.qcd.fermion.preconditioner
-    inner_kind = inv.block_cg if args.solver == "block_cg" else inv.cg
+    inner_kind = inv.block_cg if solver_kind == "block_cg" else inv.cg
     inner_cg = inner_kind({"eps": inner_tol, "maxiter": 50000})
     dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inner_cg), inner_prec, g.double),
                                eps=tol, maxiter=200)
@@ -224,7 +238,7 @@ def run_mobius_config(args, which):
             outs.append(prop(s4))
         return outs
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         one_step()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
@@ -233,14 +247,14 @@ def run_mobius_config(args, which):
     before = inner_cg.total_iterations
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         outs = one_step()
     e1.record(stream)
     torch.cuda.synchronize()
     n1 = L.gbf_launch_count()
     clk = clocks.stop()
     total_ms = e0.elapsed_time(e1)
-    inner_its = (inner_cg.total_iterations - before) // max(1, args.steps)
+    inner_its = (inner_cg.total_iterations - before) // max(1, steps)
     # device memory in use with the operators, Krylov workspace and the last
     # group's fields resident: every live allocation on the GPU, torch's and
     # the library's, as total - free after torch's cache of freed blocks is
@@ -250,18 +264,32 @@ def run_mobius_config(args, which):
     free_b, total_b = torch.cuda.mem_get_info()
     used_gb = (total_b - free_b) / 1e9
     torch_peak_gb = torch.cuda.max_memory_allocated() / 1e9
-    # true residual of the 5D systems of the last step, FP64
+    # true residual of the 5D systems of the last group, FP64 on the device
     worst = 0.0
-    for b5, x5 in last5.values():  # the last group solved
+    for b5, x5 in last5.values():
         r5 = op.F_lattice()
         op.M(r5, x5)
         g.axpby(r5, -1.0, r5, 1.0, b5)
         nr, nb = g.norm2(r5), g.norm2(b5)
         nr, nb = ([nr], [nb]) if group == 1 else (nr, nb)
         worst = max(worst, max(math.sqrt(a / b) for a, b in zip(nr, nb)))
-    value = nsrc * args.steps / (total_ms / 1000.0)
+    # and with the FP64 oracle on the host, every rhs of the last group
+    oracle_res = None
+    if oracle_residual:
+        import oracle as o
+
+        ref = o.mobius(U.host(), dims, Ls=Ls, b=1.5, c=0.5, M5=1.8, mass=mass, boundary_phases=[1, 1, 1, -1])
+        oracle_res = []
+        for b5, x5 in last5.values():
+            for k in range(group):
+                xb, bb = x5.get_natural(k), b5.get_natural(k)
+                rr = bb - ref.apply("M", xb)
+                oracle_res.append(math.sqrt(o.norm2(rr) / o.norm2(bb)))
+                del xb, bb, rr
+        del ref
+    value = nsolved * steps / (total_ms / 1000.0)
     plain = {}
-    if args.with_plain and ngroups == 1:
+    if with_plain and ngroups == 1:
         # the same packed sources with the plain method: eo2_ne CG in FP64
         # and in double-float, to the same true residual
         for name, pop in [("plain_fp64", op), ("plain_double_float", op.converted(g.double_float))]:
@@ -292,37 +320,47 @@ def run_mobius_config(args, which):
             g.axpby(r5, -1.0, r5, 1.0, b5r)
             nr, nb = g.norm2(r5), g.norm2(b5r)
             nr, nb = ([nr], [nb]) if group == 1 else (nr, nb)
-            plain[name] = {"solves_per_s": nsrc / (ms / 1000.0), "ms_per_step": ms, "cg_iterations": pcg.last.iterations,
+            plain[name] = {"solves_per_s": nsolved / (ms / 1000.0), "ms_per_step": ms, "cg_iterations": pcg.last.iterations,
                            "true_residual_5d": max(math.sqrt(a / b) for a, b in zip(nr, nb))}
             del psolve, x5, b5, xr, b5r, r5
         plain["mixed_over_plain_fp64"] = value / plain["plain_fp64"]["solves_per_s"]
         plain["mixed_over_plain_double_float"] = value / plain["plain_double_float"]["solves_per_s"]
     cfg = {"workload": f"mobius {'x'.join(map(str, dims))} Ls {Ls} b 1.5 c 0.5 M5 1.8 mass {mass} gauge eps {geps}, "
-                       f"{nsrc} {'point' if which == 'c3' else 'gaussian'} sources in {ngroups} packed group(s) of {group}, "
-                       f"propagator Export*solve*Import, defect correction ({args.inner} inner {args.solver}, tol {inner_tol}) "
-                       f"to true residual {tol}", "lattice": dims, "Ls": Ls,
+                       f"{nsolved} {'point' if which == 'c3' else 'gaussian'} sources in {ngroups} packed group(s) of "
+                       f"{group}, propagator Export*solve*Import, defect correction ({inner} inner {solver_kind}, tol "
+                       f"{inner_tol}) to true residual {tol}", "lattice": dims, "Ls": Ls,
            "l2_policy": "inputs larger than L2; no flush", "parallelism": "replicas"}
-    line = _common_line(METRIC, value, "solves/s", args, 1, total_ms, cfg, f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",
-                        {"gpu_launches": int(n1 - n0), "clocks": clk, "true_residual_5d": worst,
-                         "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
-                         "ms_per_solve": total_ms / args.steps / nsrc,
-                         "device_memory_used_gb": used_gb, "device_memory_total_gb": total_b / 1e9,
-                         "torch_peak_allocated_gb": torch_peak_gb, **plain,
-                         **({"rhs_group_tuning": rhs_tuning["results"]} if rhs_tuning else {})})
+    r = {"solves_per_s": value, "ms_per_solve": total_ms / steps / nsolved, "sources_per_step": nsolved,
+         "packed_group": group, "inner": inner, "solver": solver_kind,
+         "true_residual_5d": worst, "true_residual_oracle_max": max(oracle_res) if oracle_res else None,
+         "true_residual_oracle": oracle_res,
+         "inner_cg_iterations_per_step": inner_its, "outer_corrections": len(dc.history) - 1,
+         "device_memory_used_gb": used_gb, "device_memory_total_gb": total_b / 1e9,
+         "torch_peak_allocated_gb": torch_peak_gb, "gpu_launches": int(n1 - n0), "clocks": clk, **plain,
+         **({"rhs_group_tuning": rhs_tuning["results"]} if rhs_tuning else {})}
+    return r, total_ms, cfg
+
+
+def run_mobius_config(args, which):
+    r, total_ms, cfg = measure_mobius(which, args.warmup, args.steps, args.inner, args.solver, args.rhs_group,
+                                      args.with_plain)
+    line = _common_line(METRIC, r["solves_per_s"], "solves/s", args, 1, total_ms, cfg,
+                        f"{'f16' if args.inner == 'half' else 'f32'} inner / f64 outer",
+                        {k: v for k, v in r.items() if k != "solves_per_s"})
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_c1(args):
+def measure_c1(warmup, steps, m_reps=100):
     """c1: Wilson-clover 8^4, gauge eps 0.5, mass 0.1, csw 1.0: one Dslash (M)
     application and the plain eo2_ne CG to 1e-10 (maxiter 1000), FP64, with
-    the oracle comparison."""
+    the oracle comparison.  Returns (summary dict, total solve ms)."""
     import torch
 
     import gpt_gb300 as g
     import oracle as o
 
-    L = g.load()
+    g.load()
     dims = [8, 8, 8, 8]
     grid = g.grid(dims, g.double)
     U = g.qcd.gauge.random_su3(grid, 0.5, 8)
@@ -337,32 +375,39 @@ def run_c1(args):
     cg = inv.cg({"eps": 1e-10, "maxiter": 1000})
     slv = inv.preconditioned(pc.eo2_ne(), cg)(op)
     out = op.F_lattice()
-    for _ in range(args.warmup):
+    for _ in range(max(1, warmup)):
         op.M(out, src)
         slv(src)
     stream = torch.cuda.current_stream()
     torch.cuda.synchronize()
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     e[0].record(stream)
-    for _ in range(100):
+    for _ in range(m_reps):
         op.M(out, src)
     e[1].record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         x = slv(src)
     e[2].record(stream)
     torch.cuda.synchronize()
-    m_us = e[0].elapsed_time(e[1]) * 10.0
+    m_us = e[0].elapsed_time(e[1]) * 1000.0 / m_reps
     total_ms = e[1].elapsed_time(e[2])
     ref = o.wilson_clover(U.U, dims, **p)
-    m_err = float(np.linalg.norm(out[:] - ref.apply("M", s)) / np.linalg.norm(ref.apply("M", s)))
+    want = ref.apply("M", s)
+    m_err = float(np.linalg.norm(out[:] - want) / np.linalg.norm(want))
     xr = x[:]
     tres = float(np.sqrt(o.norm2(s - ref.apply("M", xr)) / o.norm2(s)))
+    return {"solves_per_s": steps / (total_ms / 1000.0), "ms_per_solve": total_ms / steps,
+            "M_application_us": m_us, "M_vs_oracle_rel": m_err, "cg_iterations": cg.last.iterations,
+            "true_residual_oracle": tres}, total_ms
+
+
+def run_c1(args):
+    r, total_ms = measure_c1(args.warmup, args.steps)
     cfg = {"workload": "wilson_clover 8^4 gauge eps 0.5 mass 0.1 csw 1.0 bc [1,1,1,-1], 1 gaussian source, "
-                       "one M application + plain FP64 eo2_ne CG to 1e-10", "lattice": dims,
+                       "one M application + plain FP64 eo2_ne CG to 1e-10", "lattice": [8, 8, 8, 8],
            "l2_policy": "small case: resident in L2 (reported, not a roofline number)", "parallelism": "replicas"}
-    line = _common_line(METRIC, args.steps / (total_ms / 1000.0), "solves/s", args, 1, total_ms, cfg, "f64",
-                        {"M_application_us": m_us, "M_vs_oracle_rel": m_err, "cg_iterations": cg.last.iterations,
-                         "true_residual_oracle": tres})
+    line = _common_line(METRIC, r["solves_per_s"], "solves/s", args, 1, total_ms, cfg, "f64",
+                        {k: v for k, v in r.items() if k != "solves_per_s"})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -692,18 +737,23 @@ def next_rows_measurements():
     return out
 
 
-def run_c5(args):
-    """c5: Poisson stream at 20 req/s of Wilson-clover propagator requests,
-    L in {8,16,24,32}, gauge eps U[0.2,0.5], mass U[0.01,0.2], 1-12 sources,
-    true residual 1e-10, mixed method with continuous batching, against the
-    same stream solved serially with plain FP64 CG."""
+def measure_c5(n_requests, rate=20.0):
+    """c5: Poisson stream at `rate` req/s of Wilson-clover propagator
+    requests, L in {8,16,24,32}, gauge eps U[0.2,0.5], mass U[0.01,0.2], 1-12
+    sources, true residual 1e-10, mixed method with continuous batching.
+    Beside it: (1) the same stream served strictly one request at a time with
+    the plain FP64 CG (the serial baseline), and (2) a sustainable-rate point:
+    a stream of the same mix offered at 3/4 of the request rate the server
+    reached at `rate`, where the served rate follows the offered one and the
+    latencies do not grow with the stream's length.  Returns (summary dict,
+    wall ms of the main stream, config dict)."""
     import torch
 
     import gpt_gb300 as g
     from gpt_gb300 import serving
 
     g.load()
-    reqs = serving.poisson_stream(args.requests, 20.0, seed=2026)
+    reqs = serving.poisson_stream(n_requests, rate, seed=2026)
     free, total = torch.cuda.mem_get_info()
     budget = int(0.8 * free)
     ex = serving.gpu_executor()
@@ -718,24 +768,97 @@ def run_c5(args):
     clk = clocks.stop()
     n1 = L.gbf_launch_count()
     s = serving.summarize(res, wall)
-    serial, swall = serving.Server(ex, budget, caps={8: 1, 16: 1, 24: 1, 32: 1}, method="plain", realtime=False).run(reqs)
-    # serial: one request per lattice size at a time, drained in arrival order
+
+    def above(rs):
+        return [(r.rid, r.L, r.n_src, max(r.true_residual)) for r in rs if r.true_residual and max(r.true_residual) > 1e-10]
+
+    # serial baseline: the same stream, one request at a time (max_total 1),
+    # plain FP64 eo2_ne CG, drained in arrival order
+    serial, swall = serving.Server(ex, budget, method="plain", realtime=False, max_total=1).run(reqs)
     ss = serving.summarize(serial, swall)
-    cfg = {"workload": f"serving: {args.requests} Poisson requests at 20/s, wilson_clover L^4 L in {{8,16,24,32}}, "
+    # sustainable point: the same mix offered at 3/4 of the saturated request rate
+    srate = 0.75 * s["requests_per_s"]
+    sreqs = serving.poisson_stream(n_requests, srate, seed=2027)
+    sres, sw = serving.Server(ex, budget, method="mixed").run(sreqs)
+    su = serving.summarize(sres, sw)
+    offered = n_requests / sreqs[-1].arrival
+    cfg = {"workload": f"serving: {n_requests} Poisson requests at {rate:g}/s, wilson_clover L^4 L in {{8,16,24,32}}, "
                        "gauge eps U[0.2,0.5], mass U[0.01,0.2], 1-12 gaussian sources, true residual 1e-10; "
                        "mixed method with HBM-footprint admission and batching by lattice size",
            "hbm_budget_bytes": budget, "l2_policy": "per-request working sets; no flush", "parallelism": "replicas"}
-    line = _common_line(METRIC, s["solves_per_s"], "solves/s", args, 1, 1000.0 * wall, cfg, "f32 inner / f64 outer",
-                        {"p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "requests_per_s": s["requests_per_s"],
-                         "failed": s["failed"], "max_true_residual": s["max_true_residual"], "gpu_launches": int(n1 - n0),
-                         "clocks": clk, "serial_plain_fp64": {"solves_per_s": ss["solves_per_s"], "wall_s": swall,
-                                                               "max_true_residual": ss["max_true_residual"],
-                                                               "above_tol": [(r.rid, r.L, r.n_src, max(r.true_residual))
-                                                                             for r in serial if r.true_residual and
-                                                                             max(r.true_residual) > 1e-10]},
-                         "mixed_above_tol": [(r.rid, r.L, r.n_src, max(r.true_residual)) for r in res
-                                             if r.true_residual and max(r.true_residual) > 1e-10],
-                         "speedup_vs_serial_plain": s["solves_per_s"] / ss["solves_per_s"] if ss["solves_per_s"] else None})
+    r = {"solves_per_s": s["solves_per_s"], "requests_per_s": s["requests_per_s"],
+         "offered_requests_per_s": n_requests / reqs[-1].arrival, "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
+         "failed": s["failed"], "max_true_residual": s["max_true_residual"], "mixed_above_tol": above(res),
+         "gpu_launches": int(n1 - n0), "clocks": clk,
+         "serial_plain_fp64": {"note": "the same stream served one request at a time (no overlap), plain FP64 CG",
+                               "solves_per_s": ss["solves_per_s"], "wall_s": swall, "p50_ms": ss["p50_ms"],
+                               "p99_ms": ss["p99_ms"], "max_true_residual": ss["max_true_residual"],
+                               "above_tol": above(serial)},
+         "speedup_vs_serial_plain": s["solves_per_s"] / ss["solves_per_s"] if ss["solves_per_s"] else None,
+         "sustainable_point": {"offered_requests_per_s": offered, "served_requests_per_s": su["requests_per_s"],
+                               "solves_per_s": su["solves_per_s"], "p50_ms": su["p50_ms"], "p99_ms": su["p99_ms"],
+                               "failed": su["failed"], "max_true_residual": su["max_true_residual"]}}
+    return r, 1000.0 * wall, cfg
+
+
+def other_config_measurements():
+    """The configurations beside the headline one, compact, for the default
+    line: c1 (8^4 Wilson-clover), c3 (Mobius 16^3x32 Ls 12, 12 point
+    sources, FP32 and FP16 inner), c4 (Mobius 32^3x64 Ls 16: one packed group
+    of 2 of its 12 Gaussian sources) and c5 (a 40-request serving stream).
+    Every solve's FP64 oracle residual is reported (c3, c4: every 5D system
+    of the timed step; c1: the solution)."""
+    import torch
+
+    out = {}
+
+    def clean():
+        gc.collect()
+        torch.cuda.empty_cache()
+
+    def keep(r, drop=("clocks", "rhs_group_tuning", "device_memory_total_gb", "gpu_launches")):
+        return {k: v for k, v in r.items() if k not in drop}
+
+    t0 = time.time()
+    try:
+        r, _ = measure_c1(3, 20)
+        out["c1"] = {"workload": "wilson_clover 8^4, one M + plain FP64 eo2_ne CG to 1e-10", **r}
+    except Exception as e:
+        out["c1"] = {"error": f"{type(e).__name__}: {e}"}
+    clean()
+    c3 = {"workload": "mobius 16^3x32 Ls 12, 12 point sources packed, defect correction to true residual 1e-8; "
+                      "one warm-up and one timed 12-source propagator per inner precision"}
+    for inner in ("single", "half"):
+        try:
+            r, _, _ = measure_mobius("c3", 1, 1, inner=inner)
+            c3[f"{inner}_inner"] = keep(r)
+        except Exception as e:
+            c3[f"{inner}_inner"] = {"error": f"{type(e).__name__}: {e}"}
+        clean()
+    out["c3"] = c3
+    try:
+        r, _, _ = measure_mobius("c4", 0, 1, inner="single", rhs_group=2, max_groups=1)
+        out["c4"] = {"workload": "mobius 32^3x64 Ls 16 mass 0.005, one packed group of 2 of the 12 gaussian sources, "
+                                 "FP32 inner / FP64 outer to true residual 1e-10 (first solve: includes graph capture)",
+                     "seconds_per_source": r["ms_per_solve"] / 1000.0, **keep(r)}
+    except Exception as e:
+        out["c4"] = {"error": f"{type(e).__name__}: {e}"}
+    clean()
+    try:
+        r, _, _ = measure_c5(40)
+        out["c5"] = {"workload": "serving: 40 Poisson requests at 20/s, wilson_clover L in {8,16,24,32}^4, 1-12 "
+                                 "sources each, to true residual 1e-10", **keep(r)}
+    except Exception as e:
+        out["c5"] = {"error": f"{type(e).__name__}: {e}"}
+    clean()
+    out["configs_seconds"] = time.time() - t0
+    return out
+
+
+def run_c5(args):
+    r, wall_ms, cfg = measure_c5(args.requests)
+    line = _common_line(METRIC, r["solves_per_s"], "solves/s", args, 1, wall_ms, cfg, "f32 inner / f64 outer",
+                        {k: v for k, v in r.items() if k != "solves_per_s"})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -833,24 +956,10 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ---------------------------------------------------------------------------
-# CPU restatement timing (oracle port) -- bounded samples
-# ---------------------------------------------------------------------------
-def cpu_sample_rates(op_o, src, n1=2, n2=8):
-    """Seconds per single-precision eo2_ne CG iteration and per FP64 M."""
-    t0 = time.perf_counter()
-    op_o.eo2ne_cg_single(src, 0.0, n1)
-    t1 = time.perf_counter()
-    op_o.eo2ne_cg_single(src, 0.0, n2)
-    t2 = time.perf_counter()
-    per_iter = ((t2 - t1) - (t1 - t0)) / (n2 - n1)
-    t3 = time.perf_counter()
-    op_o.apply("M", src)
-    t4 = time.perf_counter()
-    return per_iter, t4 - t3, (t2 - t0) + (t4 - t3)
-
-
 def run_reference(args, dims):
+    """--impl reference: the CPU restatement of the same mixed solve (the
+    reference's Grid CPU operator cannot be built here) on all host cores;
+    every step is one full solve of the workload, timed."""
     import oracle as o
     from gpt_gb300.qcd import gauge as G
     import gpt_gb300.core as core
@@ -866,20 +975,20 @@ def run_reference(args, dims):
     src = rng.standard_normal((V, 4, 3)) + 1j * rng.standard_normal((V, 4, 3))
     op = o.wilson_clover(U, dims, mass=CFG["mass"], csw_r=CFG["csw"], csw_t=CFG["csw"],
                          boundary_phases=CFG["phases"], with_single=True)
-    # warm-up step 1: one full CPU mixed solve gives the iteration counts
-    t0 = time.perf_counter()
-    x, inner_it, n_outer, tres = op.defect_correcting(src, CFG["tol"], 50, CFG["inner_tol"], 100000)
-    full_s = time.perf_counter() - t0
-    for _ in range(max(0, args.warmup - 1)):
-        cpu_sample_rates(op, src)
-    est = []
+
+    def solve():
+        return op.defect_correcting(src, CFG["tol"], 50, CFG["inner_tol"], 100000)
+
+    for _ in range(args.warmup):
+        solve()
+    secs = []
     tstart = time.perf_counter()
     for _ in range(args.steps):
-        per_iter, t_m, _ = cpu_sample_rates(op, src)
-        est.append(inner_it * per_iter + (n_outer + 1) * t_m)
+        t0 = time.perf_counter()
+        x, inner_it, n_outer, tres = solve()
+        secs.append(time.perf_counter() - t0)
     wall = time.perf_counter() - tstart
-    sec = statistics.median(est)
-    value = 1.0 / sec
+    value = args.steps / wall
     cores = o.num_threads()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
@@ -887,11 +996,11 @@ def run_reference(args, dims):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
         "data": "synthetic", "config": workload_config(dims),
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"per step: single-precision eo2_ne CG iterations (difference of 8 and 2) and one "
-                                   f"FP64 M, scaled by the iteration counts of one full CPU solve in warm-up "
-                                   f"({inner_it} inner iterations, {n_outer} outer, {full_s:.1f} s, true residual {tres:.2e})"},
+                         "sample": f"every step one full mixed solve on the host cores (oracle: single-precision "
+                                   f"eo2_ne CG inner, FP64 defect correction): {inner_it} inner iterations, "
+                                   f"{n_outer} outer corrections, true residual {tres:.2e}, median "
+                                   f"{statistics.median(secs):.2f} s per solve"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "cpu_full_solve_s": full_s,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -986,7 +1095,7 @@ def run_gbf(args, dims):
     h_src = torch.from_numpy(src_np.view(np.float64).reshape(-1)).pin_memory()
     h_dst = torch.empty(V * 24, dtype=torch.float64).pin_memory()
     d_nat = torch.empty(V * 24, dtype=torch.float64, device="cuda")
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = args.steps
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -1112,12 +1221,14 @@ def run_gbf(args, dims):
             xs = sol[:]
             rr = src_np - op_o.apply("M", xs)
             oracle_res[name] = math.sqrt(o.norm2(rr) / o.norm2(src_np))
-        per_iter, t_m, spent = cpu_sample_rates(op_o, src_np)
-        sec = inner_iters_per_solve * per_iter + (outer_iters + 1) * t_m
+        # one full mixed solve of the same source on the host cores, timed
+        t0 = time.perf_counter()
+        _, c_inner, c_outer, c_res = op_o.defect_correcting(src_np, CFG["tol"], 50, CFG["inner_tol"], 100000)
+        sec = time.perf_counter() - t0
         cpu = {"value": 1.0 / sec, "unit": "solves/s", "cores": o.num_threads(), "kind": "port",
-               "sample": f"single-precision eo2_ne CG iterations (difference of 8 and 2) and one FP64 M on the host, "
-                         f"scaled by this solve's {inner_iters_per_solve} inner iterations and {outer_iters} outer "
-                         f"corrections ({spent:.1f} s of CPU work)"}
+               "sample": f"one full mixed solve of this workload (oracle: single-precision eo2_ne CG inner, FP64 "
+                         f"defect correction) on the host cores: {c_inner} inner iterations, {c_outer} outer "
+                         f"corrections, {sec:.1f} s, true residual {c_res:.2e}"}
         del op_o
 
     # ---- the reference's own Dslash benchmark (benchmarks/dslash.py), after the timed region ----
@@ -1132,6 +1243,11 @@ def run_gbf(args, dims):
             nxt = next_rows_measurements()
         except Exception as e:
             nxt = {"error": f"{type(e).__name__}: {e}"}
+
+    # ---- the other configurations, compact, after the timed region ----
+    configs = {}
+    if world == 1 and not args.no_configs:
+        configs = other_config_measurements()
 
     p = sorted(step_ms)
     line = {
@@ -1149,7 +1265,7 @@ def run_gbf(args, dims):
         "data": "synthetic",
         "config": workload_config(dims),
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": V * 12 * 16,
-                "d2h_bytes_per_step": V * 12 * 16},
+                "d2h_bytes_per_step": V * 12 * 16, "steps": e2e_steps},
         "gpu_launches": int(n1 - n0),
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": "dslash_kernel<FP32 spinor, 12-real links, clover epilogue>",
@@ -1157,21 +1273,16 @@ def run_gbf(args, dims):
                      "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": d_ms},
         "cpu_baseline": cpu,
-        "p50_ms": p[len(p) // 2],
-        "p99_ms": p[min(len(p) - 1, int(math.ceil(0.99 * len(p))) - 1)],
-        "mixed": {"solves_per_s": value, "true_residual": true_res, "true_residual_oracle": oracle_res.get("mixed"),
-                  "outer_corrections": outer_iters, "inner_cg_iterations": inner_iters_per_solve},
-        "plain_fp64": {"solves_per_s": world * 1000.0 / plain_ms, "ms_per_solve": plain_ms, "cg_iterations": plain_it,
-                       "true_residual": plain_true, "true_residual_oracle": oracle_res.get("plain")},
-        "mixed_over_plain": (value / world) / (1000.0 / plain_ms),
+        # ---- detail first; the figures to read last (end of the line) ----
+        "reference_dslash_benchmark": dhop,
+        "rows_beyond_the_hot_path": nxt,
         "cg_loop": ("host-checked CUDA graphs of 16 iterations" if args.cg_graph == 0 else
                     f"host-checked CUDA graphs of {args.cg_graph} iterations" if args.cg_graph > 0 else
                     "device: one CUDA graph with a conditional while node" if args.cg_graph == -1 else
                     "no graphs: host launches with CUDA events (diagnostic)"),
-        "dslash_fp32": {"hbm_gbs": achieved, "avg_launch_ms": d_ms},
-        "dslash_fp64": {"algorithmic_gbs": fp64_gbs, "avg_launch_ms": d64_ms, "frac_of_hbm_peak": fp64_gbs / peak,
-                        "gflops_model_1320_per_site": 1320 * Vh / (d64_ms / 1000.0) / 1e9,
-                        "bound": "FP64 pipe (about 1.0 TFLOP/s measured on GB300)"},
+        "p50_ms": p[len(p) // 2],
+        "p99_ms": p[min(len(p) - 1, int(math.ceil(0.99 * len(p))) - 1)],
+        **configs,
         "double_float": {
             "note": "FP64-class precision on the FP32 pipe: every real is h + l of two FP32 words (48-bit "
                     "significand); M agrees with the FP64 operator to about 7e-15 relative",
@@ -1181,8 +1292,15 @@ def run_gbf(args, dims):
             "mixed_single_inner": {"solves_per_s": world * 1000.0 / mixed_dd_ms, "ms_per_solve": mixed_dd_ms,
                                    "true_residual_fp64": mixed_dd_true},
         },
-        "reference_dslash_benchmark": dhop,
-        "rows_beyond_the_hot_path": nxt,
+        "dslash_fp32": {"hbm_gbs": achieved, "avg_launch_ms": d_ms, "frac_of_hbm_peak": achieved / peak},
+        "dslash_fp64": {"algorithmic_gbs": fp64_gbs, "avg_launch_ms": d64_ms, "frac_of_hbm_peak": fp64_gbs / peak,
+                        "gflops_model_1320_per_site": 1320 * Vh / (d64_ms / 1000.0) / 1e9,
+                        "bound": "FP64 pipe (about 1.0 TFLOP/s measured on GB300)"},
+        "mixed": {"solves_per_s": value, "true_residual": true_res, "true_residual_oracle": oracle_res.get("mixed"),
+                  "outer_corrections": outer_iters, "inner_cg_iterations": inner_iters_per_solve},
+        "plain_fp64": {"solves_per_s": world * 1000.0 / plain_ms, "ms_per_solve": plain_ms, "cg_iterations": plain_it,
+                       "true_residual": plain_true, "true_residual_oracle": oracle_res.get("plain")},
+        "mixed_over_plain": (value / world) / (1000.0 / plain_ms),
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -15,7 +15,8 @@ GBF_EVEN, GBF_ODD, GBF_FULL = 0, 1, 2
 OPCODES = {
     "M": 2001, "Mdag": 2002, "Meooe": 2003, "MeooeDag": 2004, "Mooee": 2005, "MooeeDag": 2006,
     "MooeeInv": 2007, "MooeeInvDag": 2008, "Mdiag": 2009, "Dminus": 2010, "DminusDag": 2011,
-    "ImportPhysicalFermionSource": 2012, "ExportPhysicalFermionSolution": 2014,
+    "ImportPhysicalFermionSource": 2012, "ImportUnphysicalFermion": 2013, "ExportPhysicalFermionSolution": 2014,
+    "ExportPhysicalFermionSource": 2015,
     "Dhop": 3001, "DhopEO": 3002, "DhopDag": 4001, "DhopEODag": 4002,
 }
 

@@ -580,10 +580,35 @@ int gbf_delete(gbf_op* op) {
 int gbf_set_mass(gbf_op* op, double mass_plus, double mass_minus) {
   return guarded([&] {
     if (!op) throw Fail(GBF_E_ARG, "null operator");
-    if (!op->mobius) throw Fail(GBF_E_UNSUPPORTED, "set_mass of wilson_clover: rebuild with gbf_update_gauge");
-    op->par.mass_plus = mass_plus;
-    op->par.mass_minus = mass_minus;
-    build_smat(op);
+    if (op->mobius) {
+      op->par.mass_plus = mass_plus;
+      op->par.mass_minus = mass_minus;
+      build_smat(op);
+      op->drop_graphs();
+      return;
+    }
+    // Wilson-type operators (lib/cgpt/lib/operators/implementation.h:21-29):
+    // mass_plus is the new mass; the diagonal 4 + m (anisotropic:
+    // m + 1 + 3 nu / xi_0) moves by the difference, and a clover operator's
+    // stored clover term and its inverse are shifted and re-inverted on the
+    // device on the operator's stream
+    const double xi0 = op->par.xi_0 != 0.0 ? op->par.xi_0 : 1.0;
+    const double nu = op->par.nu != 0.0 ? op->par.nu : 1.0;
+    const double diag = mass_plus + 1.0 + 3.0 * nu / xi0;
+    const double shift = diag - op->diag;
+    if (op->has_clover && op->gauge_set && shift != 0.0) {
+      ensure_ws(op);
+      cudaStream_t s = op->stream;
+      CK(cudaMemsetAsync(op->errbits + 1, 0, sizeof(unsigned), s));
+      CK(launch_clover_shift(op->prec, op->clov[0], op->clov_inv[0], op->g.Vh, shift, op->errbits + 1, s));
+      count_launch();
+      unsigned eb = 0;
+      CK(cudaMemcpyAsync(&eb, op->errbits + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (eb != 0) throw Fail(GBF_E_ARG, "singular clover block after set_mass");
+    }
+    op->par.mass = mass_plus;
+    op->diag = diag;
     op->drop_graphs();
   });
 }
@@ -927,8 +952,14 @@ static void apply_one(gbf_op* op, int opcode, const void* src, void* dst, int sp
 }
 
 // Mobius wall transfer (4D <-> 5D) on one parity of internal fields.
+//   WALL_IMPORT          s = 0 <- P+ eta, s = Ls-1 <- P- eta (ImportUnphysicalFermion;
+//                        ImportPhysicalFermionSource applies Dminus after it)
+//   WALL_EXPORT_SOLUTION q = P- psi_0 + P+ psi_{Ls-1} (ExportPhysicalFermionSolution)
+//   WALL_EXPORT_SOURCE   q = P+ psi_0 + P- psi_{Ls-1} (ExportPhysicalFermionSource,
+//                        the adjoint of WALL_IMPORT)
+enum { WALL_EXPORT_SOLUTION = 0, WALL_IMPORT = 1, WALL_EXPORT_SOURCE = 2 };
 template <int P>
-__global__ void wall_kernel(Geo g, Geo g4, const void* in, void* out, int to5d) {
+__global__ void wall_kernel(Geo g, Geo g4, const void* in, void* out, int mode) {
   using R = typename SpinorT<P>::R;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g4.N) return;  // one thread per (4D site, rhs)
@@ -936,7 +967,7 @@ __global__ void wall_kernel(Geo g, Geo g4, const void* in, void* out, int to5d) 
   const int rhs = (int)(t - cb * g4.N5);
   const long long n0 = cb * g.N5 + (long long)rhs * g.Ls, nl = n0 + g.Ls - 1;
   cplx<R> v[12], w[12];
-  if (to5d) {
+  if (mode == WALL_IMPORT) {
     // s = 0 gets P+ eta, s = Ls-1 gets P- eta (the convention that reproduces
     // the reference's ImportPhysicalFermionSource fingerprint)
     load_spinor<P>(in, g4.N, t, v);
@@ -945,23 +976,26 @@ __global__ void wall_kernel(Geo g, Geo g4, const void* in, void* out, int to5d) 
     for (int k = 0; k < 12; ++k) w[k] = (k < 6) ? cz<R>() : v[k];
     store_spinor<P>(out, g.N, nl, w);
   } else {
-    // q = P- psi_0 + P+ psi_{Ls-1}  (lib/gpt/qcd/fermion/mobius.py:162)
-    load_spinor<P>(in, g.N, n0, v);
-    load_spinor<P>(in, g.N, nl, w);
+    // solution: q = P- psi_0 + P+ psi_{Ls-1}  (lib/gpt/qcd/fermion/mobius.py:162);
+    // source: q = P+ psi_0 + P- psi_{Ls-1}
+    const bool sol = mode == WALL_EXPORT_SOLUTION;
+    load_spinor<P>(in, g.N, sol ? n0 : nl, v);
+    load_spinor<P>(in, g.N, sol ? nl : n0, w);
     for (int k = 0; k < 6; ++k) v[k] = w[k];
     store_spinor<P>(out, g4.N, t, v);
   }
 }
 
-static void wall(gbf_op* op, const void* in, void* out, int to5d, cudaStream_t s) {
+static void wall(gbf_op* op, const void* in, void* out, int mode, cudaStream_t s) {
   const unsigned nb = (unsigned)((op->g4.N + 255) / 256);
+  const bool to5d = mode == WALL_IMPORT;
   for (int p = 0; p < 2; ++p) {
     const void* i = (const char*)in + p * (to5d ? op->half4() : op->half());
     void* o = (char*)out + p * (to5d ? op->half() : op->half4());
-    if (op->prec == P64) wall_kernel<P64><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
-    else if (op->prec == P32) wall_kernel<P32><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
-    else if (op->prec == PDD) wall_kernel<PDD><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
-    else wall_kernel<P16><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, to5d);
+    if (op->prec == P64) wall_kernel<P64><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, mode);
+    else if (op->prec == P32) wall_kernel<P32><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, mode);
+    else if (op->prec == PDD) wall_kernel<PDD><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, mode);
+    else wall_kernel<P16><<<nb, 256, 0, s>>>(op->g, op->g4, i, o, mode);
     CK(cudaGetLastError());
     count_launch();
   }
@@ -1016,17 +1050,23 @@ int gbf_apply(gbf_op* op, int opcode, const void* const* src, void* const* dst, 
     for (int i = 0; i < n; ++i) {
       if (!src[i] || !dst[i]) throw Fail(GBF_E_ARG, "null field");
       if (src[i] == dst[i]) throw Fail(GBF_E_ARG, "src and dst must differ (as in the reference)");
-      if (opcode == GBF_IMPORT_PHYSICAL_FERMION_SOURCE || opcode == GBF_EXPORT_PHYSICAL_FERMION_SOLUTION) {
+      if (opcode == GBF_IMPORT_PHYSICAL_FERMION_SOURCE || opcode == GBF_IMPORT_UNPHYSICAL_FERMION ||
+          opcode == GBF_EXPORT_PHYSICAL_FERMION_SOLUTION || opcode == GBF_EXPORT_PHYSICAL_FERMION_SOURCE) {
         if (!op->mobius) {
+          // Wilson: every import and export is a copy (reference/wilson_clover.py:165-173)
           CK(cudaMemcpyAsync(dst[i], src[i], 2 * op->half(), cudaMemcpyDeviceToDevice, s));
         } else if (opcode == GBF_IMPORT_PHYSICAL_FERMION_SOURCE) {
           // walls, then Dminus
           void* t = op->T(2);  // tmp[2], tmp[3] form one contiguous full field
           CK(cudaMemsetAsync(t, 0, 2 * op->half(), s));
-          wall(op, src[i], t, 1, s);
+          wall(op, src[i], t, WALL_IMPORT, s);
           apply_one(op, GBF_DMINUS, t, dst[i], GBF_FULL, s);
+        } else if (opcode == GBF_IMPORT_UNPHYSICAL_FERMION) {
+          // the walls alone
+          CK(cudaMemsetAsync(dst[i], 0, 2 * op->half(), s));
+          wall(op, src[i], dst[i], WALL_IMPORT, s);
         } else {
-          wall(op, src[i], dst[i], 0, s);
+          wall(op, src[i], dst[i], opcode == GBF_EXPORT_PHYSICAL_FERMION_SOLUTION ? WALL_EXPORT_SOLUTION : WALL_EXPORT_SOURCE, s);
         }
         continue;
       }

@@ -16,6 +16,7 @@
 // Roofline: HBM-bound in FP32/FP16 (per output site: 8 neighbour spinors that
 // the L2 mostly serves once, 8 links, 1 output); FP64 is bound by the FP64
 // pipe on GB300 (about 1.2 TFLOP/s measured).
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -41,6 +42,73 @@ __host__ __device__ inline unsigned dd_acc_offset16(int LK, unsigned bd) {
   if (LK == LOC_SMAT) s += (24 * (size_t)bd + kSmatWords) * 8 + 8;
   s += 2 * (size_t)bd * 8;
   return (unsigned)((s + 15) / 16);
+}
+
+// Epilogue of the hopping kernels for the 5D site n (4D site cb of the
+// output parity): out = c1 L1(hop) + c2 L2(X), store, and the per-thread
+// part of the optional reduction.  Every thread of the block calls (the
+// s-matrix op synchronises the block).
+template <int P, int LK>
+__device__ __forceinline__ void hop_epilogue(const DslashArgs& a, bool active, long long n, int cb,
+                                             cplx<typename SpinorT<P>::R> (&res)[12], double& red_re, double& red_im,
+                                             double* smem_d) {
+  using R = typename SpinorT<P>::R;
+  using V = cplx<R>;
+  const Geo& g = a.g;
+  const int p = a.out_parity;
+  if (LK == LOC_SMAT) {
+    if (a.l1.kind == LOC_SMAT) {
+      R* tile = reinterpret_cast<R*>(smem_d);
+      R* mat = tile + 24 * blockDim.x;
+      if (a.l1.cplx) smat_apply_block_c<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res);
+      else smat_apply_block<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res, true);
+    }
+  } else if (active && a.l1.kind != LOC_NONE) {
+    if constexpr (P == PDD) {
+      if (a.l1.kind == LOC_CLOVER) clover_apply_dd_lowreg(a.l1.clov[p], g.Vh, cb, res);
+      else local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
+    } else {
+      local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
+    }
+  }
+  if (active) {
+    if (a.c1 != 1.0) {
+      const R c1 = (R)a.c1;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        nrm<R>(res[k]);
+        res[k] = scl<R>(c1, res[k]);
+      }
+    }
+    if (a.X) {
+      V xv[12];
+      load_spinor<P>(a.X, g.N, n, xv);
+      if (LK != LOC_SMAT && a.l2.kind != LOC_NONE) {
+        if constexpr (P == PDD) {
+          if (a.l2.kind == LOC_CLOVER) clover_apply_dd_lowreg(a.l2.clov[p], g.Vh, cb, xv);
+          else local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+        } else {
+          local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+        }
+      }
+      const R c2 = (R)a.c2;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) res[k] = mk<R>(fma(c2, xv[k].x, res[k].x), fma(c2, xv[k].y, res[k].y));
+    }
+    store_spinor<P>(a.out, g.N, n, res);
+  }
+  if (a.red && active) {
+    double vr = 0, vi = 0;
+    if (a.red == 1) {
+      V yv[12];
+      load_spinor<P>(a.Y, g.N, n, yv);
+      site_dot<R>(yv, res, vr, vi);
+    } else {
+      vr = site_norm2<R>(res);
+    }
+    red_re += vr;
+    red_im += vi;
+  }
 }
 
 template <int P, int LS, int LK, bool LOOP>
@@ -201,61 +269,158 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
       }
     }
   }
-  // ---- epilogue ----
-  if (LK == LOC_SMAT) {
-    if (a.l1.kind == LOC_SMAT) {
-      R* tile = reinterpret_cast<R*>(smem_d);
-      R* mat = tile + 24 * blockDim.x;
-      if (a.l1.cplx) smat_apply_block_c<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res);
-      else smat_apply_block<R>(reinterpret_cast<const R*>(a.l1.smat), g.Ls, tile, mat, res, true);
-    }
-  } else if (active && a.l1.kind != LOC_NONE) {
-    if constexpr (P == PDD) {
-      if (a.l1.kind == LOC_CLOVER) clover_apply_dd_lowreg(a.l1.clov[p], g.Vh, cb, res);
-      else local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
-    } else {
-      local_apply_thread<R>(a.l1, g.Vh, p, cb, res);
-    }
+  hop_epilogue<P, LK>(a, active, n, cb, res, red_re, red_im, smem_d);
+  tile += gridDim.x;
+  } while (LOOP && tile < ntiles);
+  if (a.red) {
+    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + kSmatWords) * sizeof(R) / sizeof(double) + 1 : 0);
+    block_reduce_finalize(a.ra, red_re, red_im, g.N5, g.Ls, g.nrhs, sm);
   }
-  if (active) {
-    if (a.c1 != 1.0) {
-      const R c1 = (R)a.c1;
-#pragma unroll
-      for (int k = 0; k < 12; ++k) {
-        nrm<R>(res[k]);
-        res[k] = scl<R>(c1, res[k]);
+}
+
+// ---------------------------------------------------------------------------
+// The hop for fields with an inner extent N5 = Ls * n_rhs >= 8 (Mobius 5D
+// fields, packed right-hand sides), FP32 or FP16 spinors, 18-real FP32 links.
+// A block covers S = blockDim / N5 consecutive 4D sites with all their N5
+// inner sites (the same site -> thread mapping as dslash_kernel).  The N5
+// threads of a 4D site share its 8 neighbour indices and 8 links, so the
+// block computes them once into shared memory:
+//   nbs[j][d]  checkerboard index of the neighbour of site j in direction d
+//              (d = 2 mu + {0 forward, 1 backward});
+//   lsm[j][d]  the link of that term as a row-major 3x3 complex matrix with
+//              the boundary phase and -cc/2 folded in (the stored links),
+//              conjugate-transposed for the backward terms, so every term is
+//              the same matvec;
+// loaded coalesced (consecutive threads take consecutive sites of one link
+// component).  Each thread then streams its 8 neighbour spinors (coalesced
+// 16-byte loads along the inner index) and runs the projected matvecs.
+// Per 4D site the index arithmetic and the link loads are done once instead
+// of N5 times, and no link registers stay live across the loads.
+// ---------------------------------------------------------------------------
+constexpr int kHop5LinkStride = 41;  // float4 per site (8 links x 5, +1 pad: site rows 4 banks apart)
+
+__host__ __device__ inline size_t hop5_extra_smem(int S) {
+  return (size_t)S * kHop5LinkStride * 16 + (size_t)S * 8 * 4;
+}
+
+#ifndef GBF_HOP5_MINB
+#define GBF_HOP5_MINB 3
+#endif
+
+template <int P, int LK, bool LOOP>
+__global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashArgs a, unsigned epi_off16, int log2S) {
+  using R = float;
+  using V = float2;
+  extern __shared__ __align__(16) double smem_d[];
+  const Geo& g = a.g;
+  if (a.check_done && a.ra.st->all_done) return;
+  const int p = a.out_parity, q = 1 - p;
+  const unsigned t = threadIdx.x, bd = blockDim.x;
+  const unsigned S = 1u << log2S;
+  float4* lsm = reinterpret_cast<float4*>(smem_d) + epi_off16;
+  int* nbs = reinterpret_cast<int*>(lsm + S * kHop5LinkStride);
+  const unsigned j = g.fN5.div(t);  // 4D site of this thread within the tile
+  const unsigned i5 = t - j * (unsigned)g.N5;
+  double red_re = 0, red_im = 0;
+  const long long ntiles = (g.N + bd - 1) / bd;
+  long long tile = blockIdx.x;
+  do {
+    const int cb0 = (int)(tile << log2S);
+    // ---- neighbour indices of the S sites (bit 31: unused) ----
+    for (unsigned idx = t; idx < 8 * S; idx += bd) {
+      const int jj = idx >> 3, d = idx & 7, cbj = cb0 + jj;
+      int ycb = 0;
+      if (cbj < g.Vh) {
+        const Coord c = cb_coords(g, cbj, p);
+        const int mu = d >> 1;
+        int y[4] = {c.x[0], c.x[1], c.x[2], c.x[3]};
+        if ((d & 1) == 0) y[mu] = (y[mu] == g.L[mu] - 1) ? 0 : y[mu] + 1;
+        else y[mu] = (y[mu] == 0) ? g.L[mu] - 1 : y[mu] - 1;
+        ycb = cb_index(g, y);
+      }
+      nbs[idx] = ycb;
+    }
+    __syncthreads();
+    // ---- links: component k of link d of site jj, jj fastest (coalesced) ----
+    {
+      const float2* L2 = reinterpret_cast<const float2*>(a.links);
+      float* lf = reinterpret_cast<float*>(lsm);
+      const unsigned total = 72u * S;
+      for (unsigned idx = t; idx < total; idx += bd) {
+        const unsigned jj = idx & (S - 1), dk = idx >> log2S;
+        const unsigned d = dk / 9u, k = dk - 9u * d;
+        const int cbj = cb0 + (int)jj;
+        if (cbj >= g.Vh) continue;
+        const int mu = d >> 1;
+        const bool fwd = (d & 1) == 0;
+        const int site = fwd ? cbj : nbs[jj * 8 + d];
+        const int par = fwd ? p : q;
+        float2 v = __ldg(L2 + ((unsigned)((par * 4 + mu) * 9) + k) * (unsigned)g.Vh + (unsigned)site);
+        unsigned kk = k;
+        if (!fwd) {  // U^dagger: (i, j) <- conj (j, i)
+          kk = (k % 3u) * 3u + k / 3u;
+          v.y = -v.y;
+        }
+        *reinterpret_cast<float2*>(lf + (jj * kHop5LinkStride + d * 5u) * 4u + 2u * kk) = v;
       }
     }
-    if (a.X) {
-      V xv[12];
-      load_spinor<P>(a.X, g.N, n, xv);
-      if (LK != LOC_SMAT && a.l2.kind != LOC_NONE) {
-        if constexpr (P == PDD) {
-          if (a.l2.kind == LOC_CLOVER) clover_apply_dd_lowreg(a.l2.clov[p], g.Vh, cb, xv);
-          else local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
-        } else {
-          local_apply_thread<R>(a.l2, g.Vh, p, cb, xv);
+    __syncthreads();
+    const long long n = tile * bd + t;
+    const int cb = cb0 + (int)j;
+    const bool active = cb < g.Vh;
+    V res[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) res[k] = cz<R>();
+    if (active) {
+      const R sf = (R)a.sgn;
+      const int* nbj = nbs + j * 8;
+      const float4* lj = lsm + j * kHop5LinkStride;
+#pragma unroll
+      for (int mu = 0; mu < 4; ++mu) {
+#pragma unroll
+        for (int dir = 0; dir < 2; ++dir) {
+          const int d = 2 * mu + dir;
+          const bool fwd = dir == 0;
+          const unsigned ycb = (unsigned)nbj[d];
+          V psi[12];
+          load_spinor<P>(a.in, g.N, ycb * (unsigned)g.N5 + i5, psi);
+          const R s = fwd ? sf : -sf;
+          V h[2][3];
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int col = 0; col < 3; ++col)
+              h[r][col] = coefmadd<R>(gcoef(mu, r), s, psi[3 * gperm(mu, r) + col], psi[3 * r + col]);
+          V u[10];
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            const float4 w = lj[d * 5 + c];
+            u[2 * c] = make_float2(w.x, w.y);
+            u[2 * c + 1] = make_float2(w.z, w.w);
+          }
+          V uh[2][3];
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              V acc = cmul<R>(u[3 * i], h[r][0]);
+              acc = cmadd<R>(acc, u[3 * i + 1], h[r][1]);
+              uh[r][i] = cmadd<R>(acc, u[3 * i + 2], h[r][2]);
+            }
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) res[3 * r + i] = add<R>(res[3 * r + i], uh[r][i]);
+#pragma unroll
+          for (int r = 2; r < 4; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) res[3 * r + i] = coefmadd<R>(gcoef(mu, r), s, uh[gperm(mu, r)][i], res[3 * r + i]);
         }
       }
-      const R c2 = (R)a.c2;
-#pragma unroll
-      for (int k = 0; k < 12; ++k) res[k] = mk<R>(fma(c2, xv[k].x, res[k].x), fma(c2, xv[k].y, res[k].y));
     }
-    store_spinor<P>(a.out, g.N, n, res);
-  }
-  if (a.red && active) {
-    double vr = 0, vi = 0;
-    if (a.red == 1) {
-      V yv[12];
-      load_spinor<P>(a.Y, g.N, n, yv);
-      site_dot<R>(yv, res, vr, vi);
-    } else {
-      vr = site_norm2<R>(res);
-    }
-    red_re += vr;
-    red_im += vi;
-  }
-  tile += gridDim.x;
+    hop_epilogue<P, LK>(a, active, n, cb, res, red_re, red_im, smem_d);
+    tile += gridDim.x;
+    if (LOOP) __syncthreads();  // the next tile overwrites nbs and lsm
   } while (LOOP && tile < ntiles);
   if (a.red) {
     double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + kSmatWords) * sizeof(R) / sizeof(double) + 1 : 0);
@@ -354,6 +519,35 @@ static cudaError_t launch_tl(const DslashArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// hop5: the epilogue's shared memory first, then the links and indices
+template <int P, int LK, bool LOOP>
+static cudaError_t launch_hop5_tl(const DslashArgs& a, int bd, cudaStream_t st) {
+  const int S = bd / a.g.N5;
+  int log2S = 0;
+  while ((1 << log2S) < S) ++log2S;
+  const size_t epi = dslash_smem_bytes(P, LK, bd);
+  const unsigned off16 = (unsigned)((epi + 15) / 16);
+  const size_t sm = 16 * (size_t)off16 + hop5_extra_smem(S);
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  auto k = hop5_kernel<P, LK, LOOP>;
+  const int res = resident_blocks((const void*)k, bd, sm);
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs, res) : ntiles;
+  k<<<(unsigned)nb, bd, sm, st>>>(a, off16, log2S);
+  return cudaGetLastError();
+}
+
+template <int P, int LK>
+static cudaError_t launch_hop5(const DslashArgs& a, cudaStream_t st) {
+  const int bd = pick_bd(a.bd, a.g.N5);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const int S = bd / a.g.N5;
+  const size_t sm = 16 * ((dslash_smem_bytes(P, LK, bd) + 15) / 16) + hop5_extra_smem(S);
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const int res = resident_blocks((const void*)hop5_kernel<P, LK, true>, bd, sm);
+  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs, res) < ntiles;
+  return loop ? launch_hop5_tl<P, LK, true>(a, bd, st) : launch_hop5_tl<P, LK, false>(a, bd, st);
+}
+
 template <int P, int LS, int LK>
 static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
@@ -364,8 +558,23 @@ static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
   return loop ? launch_tl<P, LS, LK, true>(a, st) : launch_tl<P, LS, LK, false>(a, st);
 }
 
+// GBF_HOP5=0 in the environment selects the per-thread hop for every field
+// (a switch for comparing the two kernels; results are bitwise equal)
+static bool hop5_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBF_HOP5");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st) {
   const int LK = (a.l1.kind == LOC_SMAT || a.l2.kind == LOC_SMAT) ? LOC_SMAT : LOC_CLOVER;
+  // fields with an inner extent of 8 or more: the shared-memory link hop
+  if (hop5_enabled() && a.g.N5 >= 8 && LS == L32 && (P == P32 || P == P16)) {
+    if (P == P32) return LK == LOC_SMAT ? launch_hop5<P32, LOC_SMAT>(a, st) : launch_hop5<P32, LOC_CLOVER>(a, st);
+    return LK == LOC_SMAT ? launch_hop5<P16, LOC_SMAT>(a, st) : launch_hop5<P16, LOC_CLOVER>(a, st);
+  }
 #define GBF_D(PP, LL)                                                     \
   if (P == PP && LS == LL) {                                             \
     if (LK == LOC_SMAT) return launch_t<PP, LL, LOC_SMAT>(a, st);        \

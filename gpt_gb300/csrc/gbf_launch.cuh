@@ -94,6 +94,11 @@ cudaError_t launch_pack_links(int LS, const Geo& g, const double2* U, void* link
 cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double csw_r, double csw_t, void* c64, void* ci64,
                           void* c32, void* ci32, unsigned* err_bits, cudaStream_t st);
 
+// set_mass of a clover operator: clover diagonal += shift (both parities and
+// blocks, in place, in the operator's storage precision) and the inverse
+// blocks rebuilt; err receives a large value for a singular block
+cudaError_t launch_clover_shift(int prec, void* clov, void* clov_inv, int Vh, double shift, unsigned* err, cudaStream_t st);
+
 // FP64 clover storage (double2 [2*nrows32][Vh]) -> FP32 (float4 [nrows32][Vh]);
 // nrows32 is a row count (18 per parity block), not an element count
 cudaError_t launch_clover_narrow(const void* src64, void* dst32, long long nrows32, int Vh, cudaStream_t st);

@@ -636,6 +636,97 @@ cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double cs
   return cudaGetLastError();
 }
 
+// Mass change of a clover operator (set_mass): add `shift` to the diagonal
+// of both chiral blocks of every site's clover term, in place, and rebuild
+// the inverse blocks (Gauss-Jordan with partial pivoting in FP64; the
+// matrices of one thread live in shared memory).  One thread per (site,
+// parity, block); `prec` is the storage of the operator (P64 double2
+// [36][Vh], P32 / P16 float4 [18][Vh], PDD float4 [36][Vh] per parity).
+constexpr int kShiftBlock = 32;
+__device__ __forceinline__ void clover_row_load(int prec, const void* base, int Vh, size_t off_rows, int b, int cb,
+                                                double (&re)[36]) {
+  if (prec == P64) {
+    const double2* p = reinterpret_cast<const double2*>(base) + off_rows * 2 * Vh;
+    for (int k = 0; k < 18; ++k) {
+      const double2 q = p[(size_t)(18 * b + k) * Vh + cb];
+      re[2 * k] = q.x;
+      re[2 * k + 1] = q.y;
+    }
+  } else if (prec == PDD) {
+    const float4* p = reinterpret_cast<const float4*>(base) + off_rows * 2 * Vh;
+    for (int k = 0; k < 18; ++k) {
+      const float4 q = p[(size_t)(18 * b + k) * Vh + cb];
+      re[2 * k] = (double)q.x + (double)q.z;
+      re[2 * k + 1] = (double)q.y + (double)q.w;
+    }
+  } else {
+    const float4* p = reinterpret_cast<const float4*>(base) + off_rows * Vh;
+    for (int k = 0; k < 9; ++k) {
+      const float4 q = p[(size_t)(9 * b + k) * Vh + cb];
+      re[4 * k] = q.x; re[4 * k + 1] = q.y; re[4 * k + 2] = q.z; re[4 * k + 3] = q.w;
+    }
+  }
+}
+__device__ __forceinline__ void clover_row_store(int prec, void* base, int Vh, size_t off_rows, int b, int cb,
+                                                 const double (&re)[36]) {
+  if (prec == P64) {
+    double2* p = reinterpret_cast<double2*>(base) + off_rows * 2 * Vh;
+    for (int k = 0; k < 18; ++k) p[(size_t)(18 * b + k) * Vh + cb] = make_double2(re[2 * k], re[2 * k + 1]);
+  } else if (prec == PDD) {
+    float4* p = reinterpret_cast<float4*>(base) + off_rows * 2 * Vh;
+    for (int k = 0; k < 18; ++k) {
+      const dd x(re[2 * k]), y(re[2 * k + 1]);
+      p[(size_t)(18 * b + k) * Vh + cb] = make_float4(x.h, y.h, x.l, y.l);
+    }
+  } else {
+    float4* p = reinterpret_cast<float4*>(base) + off_rows * Vh;
+    for (int k = 0; k < 9; ++k)
+      p[(size_t)(9 * b + k) * Vh + cb] =
+          make_float4((float)re[4 * k], (float)re[4 * k + 1], (float)re[4 * k + 2], (float)re[4 * k + 3]);
+  }
+}
+
+__global__ void __launch_bounds__(kShiftBlock) clover_shift_kernel(int prec, void* clov, void* clov_inv, int Vh,
+                                                                     double shift, unsigned* err) {
+  __shared__ double2 sA[kShiftBlock][36], sI[kShiftBlock][36];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4LL * Vh) return;
+  const int cb = (int)(t % Vh);
+  const int pb = (int)(t / Vh);  // parity * 2 + block
+  const int par = pb >> 1, b = pb & 1;
+  // rows of one parity: 36 (FP64 and double-float, in 16-byte units of the
+  // storage) or 18 (FP32 float4); offsets in units of the storage row / 2
+  const size_t off = (size_t)par * 18;
+  double re[36];
+  clover_row_load(prec, clov, Vh, off, b, cb, re);
+  for (int i = 0; i < 6; ++i) re[i] += shift;
+  clover_row_store(prec, clov, Vh, off, b, cb, re);
+  double2(&A)[36] = sA[threadIdx.x];
+  double2(&I)[36] = sI[threadIdx.x];
+  for (int i = 0; i < 6; ++i) A[7 * i] = make_double2(re[i], 0.0);
+  for (int i = 1; i < 6; ++i)
+    for (int j = 0; j < i; ++j) {
+      const double2 v = make_double2(re[6 + 2 * tri(i, j)], re[6 + 2 * tri(i, j) + 1]);
+      A[6 * i + j] = v;
+      A[6 * j + i] = zconj(v);
+    }
+  if (!invert6(A, I)) atomic_max_err(err, 1e30);
+  for (int i = 0; i < 6; ++i) re[i] = I[7 * i].x;
+  for (int i = 1; i < 6; ++i)
+    for (int j = 0; j < i; ++j) {
+      re[6 + 2 * tri(i, j)] = I[6 * i + j].x;
+      re[6 + 2 * tri(i, j) + 1] = I[6 * i + j].y;
+    }
+  clover_row_store(prec, clov_inv, Vh, off, b, cb, re);
+}
+
+cudaError_t launch_clover_shift(int prec, void* clov, void* clov_inv, int Vh, double shift, unsigned* err, cudaStream_t st) {
+  const long long n = 4LL * Vh;
+  clover_shift_kernel<<<(unsigned)((n + kShiftBlock - 1) / kShiftBlock), kShiftBlock, 0, st>>>(prec, clov, clov_inv, Vh,
+                                                                                               shift, err);
+  return cudaGetLastError();
+}
+
 __global__ void clover_narrow_kernel(const double2* src, float4* dst, long long nrows32, int Vh) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrows32 * Vh) return;

@@ -41,8 +41,18 @@ class matrix_operator:
     def __mul__(self, src):
         return self(src)
 
+    def _with_dst(self, new_dst, new_dst_adj):
+        if new_dst is not None:
+            self._new_dst = new_dst
+        self._new_dst_adj = new_dst_adj
+        return self
+
     def adj(self):
-        return matrix_operator(self.adj_mat, self.mat, self.adj_inv_mat, self.inv_mat)
+        # operators between different vector spaces (the 4D <-> 5D imports and
+        # exports) create the adjoint's destination in the other space
+        nd = getattr(self, "_new_dst_adj", None)
+        od = self.__dict__.get("_new_dst")
+        return matrix_operator(self.adj_mat, self.mat, self.adj_inv_mat, self.inv_mat)._with_dst(nd, od)
 
     def inv(self):
         return matrix_operator(self.inv_mat, self.adj_inv_mat, self.mat, self.adj_mat)
@@ -137,17 +147,16 @@ class fermion_operator(matrix_operator):
         elif src.cb is not core.full:
             dst.cb = src.cb
 
-    def _op(self, name, name_dag, new_dst=None, inv=None, inv_dag=None):
+    def _op(self, name, name_dag, new_dst=None, inv=None, inv_dag=None, new_dst_adj=None):
         def m(n):
             return (lambda dst, src: self._apply(n, dst, src)) if n else None
 
         a, ad, i, idg = m(name), m(name_dag), m(inv), m(inv_dag)
         if self.daggered:
             a, ad, i, idg = ad, a, idg, i
-        op = matrix_operator(a, ad, i, idg)
-        if new_dst is not None:
-            op._new_dst = new_dst
-        return op
+            if new_dst_adj is not None:
+                new_dst, new_dst_adj = new_dst_adj, new_dst
+        return matrix_operator(a, ad, i, idg)._with_dst(new_dst, new_dst_adj)
 
     def _register(self):
         # base.py:84-169 (method registry)
@@ -166,6 +175,12 @@ class fermion_operator(matrix_operator):
         to_U = lambda src: self.U_lattice()
         self.ImportPhysicalFermionSource = self._op("ImportPhysicalFermionSource", None, new_dst=to_F)
         self.ExportPhysicalFermionSolution = self._op("ExportPhysicalFermionSolution", None, new_dst=to_U)
+        # opcodes 2013 / 2015 (base.py:147-164): the walls of the physical
+        # import without Dminus, and its adjoint
+        self.ImportUnphysicalFermion = self._op("ImportUnphysicalFermion", "ExportPhysicalFermionSource",
+                                                new_dst=to_F, new_dst_adj=to_U)
+        self.ExportPhysicalFermionSource = self._op("ExportPhysicalFermionSource", "ImportUnphysicalFermion",
+                                                    new_dst=to_U, new_dst_adj=to_F)
 
     # ---- base.py:219-260 ----
     def converted(self, precision):
@@ -338,8 +353,10 @@ def mobius(U, params=None, **kw):
     if p.get("mass") is not None:
         p["mass_plus"] = p["mass"]
         p["mass_minus"] = p["mass"]
-    if "omega" in p:
-        raise NotImplementedError("zmobius (omega) is not implemented on this path")
+    if p.get("omega") is not None:
+        # per-slice Cayley coefficients from omega (the c_s of
+        # mobius.py:34-46 with omega): the zmobius operator
+        return zmobius(U, p)
     p.setdefault("n_rhs", 1)
     return mobius_operator(U, p)
 

@@ -114,12 +114,15 @@ def default_caps(sizes=(8, 16, 24, 32)):
 
 
 class Server:
-    def __init__(self, executor, hbm_budget_bytes, caps=None, method="mixed", realtime=True):
+    def __init__(self, executor, hbm_budget_bytes, caps=None, method="mixed", realtime=True, max_total=None):
         """executor(request, method) -> Result fields (dict); runs on the
-        calling worker thread with its own CUDA stream."""
+        calling worker thread with its own CUDA stream.  caps: concurrent
+        requests per lattice size; max_total: concurrent requests over all
+        sizes (1 serves the stream strictly one request at a time)."""
         self.executor = executor
         self.budget = HBMBudget(hbm_budget_bytes)
         self.caps = caps or default_caps()
+        self.max_total = max_total
         self.method = method
         self.realtime = realtime
         self.lock = threading.Condition()
@@ -169,7 +172,8 @@ class Server:
                         if r.L != L:
                             continue
                         nb = footprint_bytes(r.L, r.n_src, self.method)
-                        if self.running[L] < self.caps.get(L, 2) and self.budget.fits(nb):
+                        total_ok = self.max_total is None or sum(self.running.values()) < self.max_total
+                        if total_ok and self.running[L] < self.caps.get(L, 2) and self.budget.fits(nb):
                             waiting.remove(r)
                             self.budget.acquire(nb)
                             self.running[L] += 1

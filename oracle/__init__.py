@@ -34,7 +34,8 @@ _lib = None
 OPCODES = {
     "M": 2001, "Mdag": 2002, "Meooe": 2003, "MeooeDag": 2004, "Mooee": 2005, "MooeeDag": 2006,
     "MooeeInv": 2007, "MooeeInvDag": 2008, "Mdiag": 2009, "Dminus": 2010, "DminusDag": 2011,
-    "ImportPhysicalFermionSource": 2012, "ExportPhysicalFermionSolution": 2014,
+    "ImportPhysicalFermionSource": 2012, "ImportUnphysicalFermion": 2013, "ExportPhysicalFermionSolution": 2014,
+    "ExportPhysicalFermionSource": 2015,
     "Dhop": 3001, "DhopDag": 4001,
 }
 EVEN, ODD, FULL = 0, 1, 2
@@ -350,6 +351,18 @@ class mobius(_op):
         x5 = np.ascontiguousarray(x5, dtype=np.complex128)
         out = np.zeros((self.V, 4, 3), dtype=np.complex128)
         _check(lib().orc_op_apply(self.obj, OPCODES["ExportPhysicalFermionSolution"], _ptr(x5), _ptr(out), FULL))
+        return out
+
+    def import_unphysical(self, src4):
+        """Opcode 2013: the walls of the physical import (P+ eta on s = 0,
+        P- eta on s = Ls-1) without Dminus."""
+        return self.import_physical_source(src4, variant=self.IMPORT_VARIANT & 1)
+
+    def export_physical_source(self, x5):
+        """Opcode 2015: P+ psi_0 + P- psi_{Ls-1}, the adjoint of import_unphysical."""
+        x5 = np.ascontiguousarray(x5, dtype=np.complex128)
+        out = np.zeros((self.V, 4, 3), dtype=np.complex128)
+        _check(lib().orc_op_apply(self.obj, OPCODES["ExportPhysicalFermionSource"], _ptr(x5), _ptr(out), FULL))
         return out
 
 

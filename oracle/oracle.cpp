@@ -757,7 +757,8 @@ static bool invert_cmat(int n, const cd* A, cd* Ainv) {
 enum {
   OP_M = 2001, OP_MDAG = 2002, OP_MEOOE = 2003, OP_MEOOE_DAG = 2004, OP_MOOEE = 2005, OP_MOOEE_DAG = 2006,
   OP_MOOEE_INV = 2007, OP_MOOEE_INV_DAG = 2008, OP_MDIAG = 2009, OP_DMINUS = 2010, OP_DMINUS_DAG = 2011,
-  OP_IMPORT_PHYS_SRC = 2012, OP_EXPORT_PHYS_SOL = 2014, OP_DHOP = 3001, OP_DHOP_DAG = 4001
+  OP_IMPORT_PHYS_SRC = 2012, OP_IMPORT_UNPHYS = 2013, OP_EXPORT_PHYS_SOL = 2014, OP_EXPORT_PHYS_SRC = 2015,
+  OP_DHOP = 3001, OP_DHOP_DAG = 4001
 };
 
 // Common interface used by the even-odd solver: all fields are natural
@@ -1304,14 +1305,26 @@ int orc_op_apply(void* o, int opcode, const double* in, double* out, int parity)
         }
         return;
       }
-      if (opcode == OP_EXPORT_PHYS_SOL) {
-        // q = P- psi_0 + P+ psi_{Ls-1}
+      if (opcode == OP_EXPORT_PHYS_SOL || opcode == OP_EXPORT_PHYS_SRC) {
+        // solution: q = P- psi_0 + P+ psi_{Ls-1} (lib/gpt/qcd/fermion/mobius.py:162);
+        // source (opcode 2015, lib/gpt/qcd/fermion/operator/base.py:159-164):
+        // q = P+ psi_0 + P- psi_{Ls-1}, the adjoint of the wall placement of
+        // the import (lib/gpt/qcd/fermion/preconditioner/physical.py:36-39
+        // composes it with Dminus^+ as the adjoint of the physical import)
+        const bool sol = opcode == OP_EXPORT_PHYS_SOL;
 #pragma omp parallel for
         for (long x = 0; x < G.V; ++x)
-          for (int k = 0; k < 12; ++k) out_[x * 12 + k] = (k < 6) ? i[((size_t)x * Ls + Ls - 1) * 12 + k] : i[((size_t)x * Ls) * 12 + k];
+          for (int k = 0; k < 12; ++k) {
+            const bool from_last = (k < 6) == sol;
+            out_[x * 12 + k] = i[((size_t)x * Ls + (from_last ? Ls - 1 : 0)) * 12 + k];
+          }
         return;
       }
-      if (opcode == OP_IMPORT_PHYS_SRC) throw std::runtime_error("use orc_mobius_import");
+      if (opcode == OP_IMPORT_PHYS_SRC || opcode == OP_IMPORT_UNPHYS) throw std::runtime_error("use orc_mobius_import");
+    } else if (opcode >= OP_IMPORT_PHYS_SRC && opcode <= OP_EXPORT_PHYS_SRC) {
+      // Wilson: every import and export is a copy (lib/gpt/qcd/fermion/reference/wilson_clover.py:165-173)
+      std::memcpy(out_, i, (size_t)op.G->V * 12 * sizeof(cd));
+      return;
     }
     apply_full(op.d.get(), opcode, out_, i, parity);
   });

@@ -74,10 +74,13 @@ def test_structs_match_the_c_compiler(tmp_path):
     assert got == want
 
 
-def test_wilson_clover_parameter_handling():
+def test_wilson_clover_parameter_handling(monkeypatch):
     from gpt_gb300.qcd import fermion
 
     with pytest.raises(ValueError):
         fermion.wilson_clover(None, {"mass": 0.1, "cF": 1.3, "boundary_phases": [1, 1, 1, -1]})
-    with pytest.raises(NotImplementedError):
-        fermion.mobius(None, {"omega": [1.0], "mass": 0.1})
+    # mobius with per-slice omega is the zmobius operator
+    seen = {}
+    monkeypatch.setattr(fermion, "zmobius", lambda U, p: seen.setdefault("p", p))
+    fermion.mobius(None, {"omega": [1.0, 0.5], "mass": 0.1, "b": 1.0, "c": 0.0, "M5": 1.8})
+    assert seen["p"]["omega"] == [1.0, 0.5]

@@ -154,6 +154,9 @@ MOB = dict(Ls=6, b=1.5, c=0.5, M5=1.8, mass_plus=0.05, mass_minus=0.09, boundary
 TM = dict(mass=0.1, mu=0.3, boundary_phases=[1.0, 1.0, 1.0, -1.0])
 ZMOB = dict(omega=[0.8 + 0.3j, 1.1 - 0.2j, 0.6, 1.4 + 0.1j], b=1.2, c=0.3, M5=1.8, mass=0.07,
             boundary_phases=[1.0, 1.0, 1.0, -1.0])
+# inner extents Ls * n_rhs >= 8 run the shared-memory link hop in FP32/FP16
+MOB8 = dict(MOB, Ls=8)
+ZMOB8 = dict(ZMOB, omega=ZMOB["omega"] + [0.9 - 0.1j, 1.2, 0.7 + 0.2j, 1.05])
 
 
 def _oracle(kind, U, dims, p):
@@ -172,8 +175,10 @@ def _oracle(kind, U, dims, p):
     ("wilson_clover", WC_ANISO, [4, 2, 6, 4]),
     ("wilson_clover", dict(mass=0.3, boundary_phases=[1, 1, 1, -1]), [2, 2, 2, 2]),
     ("mobius", MOB, [4, 4, 2, 4]),
+    ("mobius", MOB8, [4, 2, 6, 4]),
     ("wilson_twisted_mass", TM, [4, 4, 4, 8]),
     ("zmobius", ZMOB, [4, 4, 2, 4]),
+    ("zmobius", ZMOB8, [4, 4, 2, 4]),
 ])
 def test_opcodes_vs_oracle(kind, params, dims, prec):
     P = PREC[prec]
@@ -214,6 +219,13 @@ def test_mobius_import_export(prec, kind, params):
     s5 = rand_field(ref.shape(), 2)
     q = op.ExportPhysicalFermionSolution(to_gpu(op, s5))
     assert rel(q[:], ref.export_physical_solution(s5)) < TOL[prec]
+    # opcodes 2013 / 2015: the walls alone, and their adjoint
+    u = op.ImportUnphysicalFermion(to_gpu(op, s4, five=False))
+    assert rel(u[:], ref.import_unphysical(s4)) < TOL[prec]
+    e = op.ExportPhysicalFermionSource(to_gpu(op, s5))
+    assert rel(e[:], ref.export_physical_source(s5)) < TOL[prec]
+    e2 = op.ImportUnphysicalFermion.adj()(to_gpu(op, s5))
+    assert np.array_equal(e2[:], e[:])
 
 
 def test_reconstruct12_matches_full_links():
@@ -333,6 +345,41 @@ def test_packed_multi_rhs_cg_equals_separate_solves(kind, params, nrhs):
         its.append(cgs.last.iterations)
         assert rel(X.get_natural(k), x) < 1e-12
     assert cgp.last.iterations == max(its)
+
+
+@pytest.mark.parametrize("kind,params,nrhs,dims", [
+    ("wilson_clover", WC, 8, [4, 4, 4, 8]),
+    ("wilson_clover", WC, 12, [8, 4, 4, 4]),
+    ("mobius", dict(MOB, mass_plus=0.1, mass_minus=0.1), 2, [4, 4, 4, 8]),
+    # 2048 tiles of one 4D site: more than a wave of resident blocks, so the
+    # reducing launches loop over tiles
+    ("mobius", dict(MOB, Ls=12, mass_plus=0.1, mass_minus=0.1), 12, [8, 8, 8, 8]),
+])
+def test_packed_single_precision_inner_solve_vs_oracle(kind, params, nrhs, dims):
+    """Packed right-hand sides with an FP32 inner operator (the shared-memory
+    link hop, reducing launches included): M per rhs within the FP32
+    tolerance, and the defect-corrected mixed solve of every rhs to the FP64
+    oracle's true residual 1e-10."""
+    U = g.qcd.gauge.random_su3(g.grid(dims), 0.4, 31).U
+    ref = _oracle(kind, U, dims, params)
+    packed = gpu_op(kind, U, dims, g.double, n_rhs=nrhs, **params)
+    p32 = packed.converted(g.single)
+    srcs = [rand_field(ref.shape(), 60 + k) for k in range(nrhs)]
+    P, P32 = packed.F_lattice(), p32.F_lattice()
+    for k in range(nrhs):
+        P.set_natural(srcs[k], k)
+        P32.set_natural(srcs[k], k)
+    out = p32.M(P32)
+    for k in range(nrhs):
+        assert rel(out.get_natural(k), ref.apply("M", srcs[k])) < TOL["single"], k
+    inv = g.algorithms.inverter
+    pc = g.qcd.fermion.preconditioner
+    dc = inv.defect_correcting(inv.mixed_precision(inv.preconditioned(pc.eo2_ne(), inv.cg({"eps": 1e-5, "maxiter": 4000})),
+                                                   g.single, g.double), eps=1e-10, maxiter=40)
+    X = dc(packed)(P)
+    for k in range(nrhs):
+        r = srcs[k] - ref.apply("M", X.get_natural(k))
+        assert np.sqrt(o.norm2(r) / o.norm2(srcs[k])) < 1e-10, k
 
 
 def test_half_precision_storage_operator():

@@ -168,6 +168,36 @@ def test_eo_decomposition_identities():
             assert np.linalg.norm((y - s)[mask]) / np.linalg.norm(s[mask]) < 1e-13
 
 
+def test_unphysical_import_and_physical_source_export():
+    """Opcodes 2013 and 2015 (lib/gpt/qcd/fermion/operator/base.py:147-164):
+    ImportPhysicalFermionSource = Dminus ImportUnphysicalFermion (its wall
+    placement is pinned by the reference's .ImportPhysicalFermionSource
+    fingerprint above), and ExportPhysicalFermionSource is the adjoint of
+    ImportUnphysicalFermion, as lib/gpt/qcd/fermion/preconditioner/physical.py:36-39
+    uses it (the adjoint of the physical import = ExportPhysicalFermionSource
+    Dminus^+).  Wilson: both are copies."""
+    dims = [4, 4, 2, 4]
+    U = o.synthetic_gauge(dims, 0.4, 5)
+    rng = np.random.default_rng(8)
+    V = int(np.prod(dims))
+    e = rng.standard_normal((V, 4, 3)) + 1j * rng.standard_normal((V, 4, 3))
+    for m in [o.mobius(U, dims, Ls=6, b=1.5, c=0.5, M5=1.8, mass=0.1),
+              o.zmobius(U, dims, omega=[0.8 + 0.3j, 1.1, 0.6 - 0.1j, 1.4], b=1.2, c=0.3, M5=1.8, mass=0.07)]:
+        p = rng.standard_normal(m.shape()) + 1j * rng.standard_normal(m.shape())
+        a = o.inner(m.import_unphysical(e), p)
+        b = o.inner(e, m.export_physical_source(p))
+        assert abs(a - b) / abs(a) < 1e-14
+        y = m.import_physical_source(e)
+        assert np.linalg.norm(m.apply("Dminus", m.import_unphysical(e)) - y) / np.linalg.norm(y) < 1e-15
+        # physical.py:36-39: <Import_phys e, p> = <e, ExportSource(Dminus^+ p)>
+        c = o.inner(y, p)
+        d = o.inner(e, m.export_physical_source(m.apply("DminusDag", p)))
+        assert abs(c - d) / abs(c) < 1e-13
+    w = o.wilson_clover(U, dims, mass=0.1, csw_r=1.0, csw_t=1.0)
+    for name in ["ImportUnphysicalFermion", "ExportPhysicalFermionSource"]:
+        assert np.array_equal(w.apply(name, e), e)
+
+
 def test_oracle_solvers_true_residual():
     dims = [4, 4, 4, 8]
     U = o.synthetic_gauge(dims, 0.5, 3)
