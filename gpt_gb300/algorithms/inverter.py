@@ -20,11 +20,15 @@ class cg:
     equations; convergence when |r|^2 <= eps^2 |b|^2 (cg.py:70, 103)."""
 
     def __init__(self, params=None, eps=1e-15, maxiter=1000000, fail_if_not_converged=False, iterations_per_graph=0,
-                 profile=False):
+                 profile=False, eps_abs=None, miniter=0, prec=None):
         p = dict(params or {})
         self.eps = p.get("eps", eps)
         self.maxiter = p.get("maxiter", maxiter)
         self.fail_if_not_converged = p.get("fail_if_not_converged", fail_if_not_converged)
+        # for the generic CG on any matrix operator (cg.py:25-34)
+        self.eps_abs = p.get("eps_abs", eps_abs)
+        self.miniter = p.get("miniter", miniter)
+        self.prec = p.get("prec", prec)
         # iterations_per_graph K > 0: CUDA graphs of K iterations with a host
         # convergence check between them; 0: the library's default K (16);
         # -1: the whole CG loop on the device (one CUDA graph with a
@@ -38,21 +42,25 @@ class cg:
 
     def modified(self, **params):
         d = dict(eps=self.eps, maxiter=self.maxiter, fail_if_not_converged=self.fail_if_not_converged,
-                 iterations_per_graph=self.iterations_per_graph, profile=self.profile)
+                 iterations_per_graph=self.iterations_per_graph, profile=self.profile, eps_abs=self.eps_abs,
+                 miniter=self.miniter, prec=self.prec)
         d.update(params)
         return cg(d)
 
     def __call__(self, mat):
-        """cg(mat) for the eo2_ne normal operator of a native operator
-        (preconditioner.eo2_ne()(op).Mpc): CG on the device starting from the
-        destination as the guess (gbf_solve_normal_cg; the reference's
-        guess handling, cg.py:48-68: r = src - mat psi, zero source -> zero
-        solution).  A guess that already meets the tolerance returns after
-        zero iterations."""
+        """cg(mat).  For the eo2_ne normal operator of a native operator
+        (preconditioner.eo2_ne()(op).Mpc): the whole CG on the device starting
+        from the destination as the guess (gbf_solve_normal_cg; the
+        reference's guess handling, cg.py:48-68: r = src - mat psi, zero
+        source -> zero solution); a guess that already meets the tolerance
+        returns after zero iterations.  For any other Hermitian positive
+        definite matrix operator (a composed or shifted operator, a user
+        operator): the recursion of cg.py:47-105 driven from the host, every
+        vector operation and reduction on the device (norm2, inner_product,
+        axpy_norm2, axpby), the matrix applied through its own callable."""
         op = getattr(mat, "native_op", None)
         if op is None:
-            raise NotImplementedError("cg runs on the device for preconditioner.eo2_ne()(op).Mpc or through "
-                                      "preconditioned(eo2_ne(), cg(...))")
+            return self._generic(mat)
         import ctypes
 
         from .. import _lib
@@ -73,6 +81,87 @@ class cg:
 
         m = _fermion.matrix_operator(inv, inv_mat=mat.mat)
         m._new_dst = lambda src: op.F_lattice(core.odd)
+        m.accept_guess = True
+        return m
+
+
+    def _generic(self, mat):
+        import types
+
+        me = self
+        apply = mat.mat if hasattr(mat, "mat") and mat.mat is not None else mat
+        prec = self.prec(mat) if self.prec is not None else None
+
+        def per_rhs(v, n):
+            return list(v) if isinstance(v, (list, tuple)) else [v] * n
+
+        def inv(psi, src):
+            if src is psi:
+                raise ValueError("src and psi must differ (cg.py:49)")
+            n = src.layout.n_rhs
+            p, mmp, r = src.new(), src.new(), src.new()
+            z = src.new() if prec is not None else None
+            apply(mmp, psi)
+            core.axpby(r, -1.0, mmp, 1.0, src)
+            if prec is not None:
+                z[:] = 0
+                prec(z, r)
+                core.copy(p, z)
+                cp = [x.real for x in per_rhs(core.inner_product(r, z), n)]
+            else:
+                core.copy(p, r)
+                cp = per_rhs(core.norm2(p), n)
+            ssq = per_rhs(core.norm2(src), n)
+            res_info = types.SimpleNamespace(iterations=0, converged=0, breakdown=0,
+                                             residual_sq=[0.0] * n)
+            me.last = res_info
+            me.history = []
+            if all(v == 0.0 for v in ssq):
+                psi[:] = 0
+                res_info.converged = 1
+                return
+            rsq = [me.eps ** 2 * v for v in ssq]
+            done = [False] * n
+            for k in range(me.maxiter):
+                c = cp
+                apply(mmp, p)
+                d = [x.real for x in per_rhs(core.inner_product(p, mmp), n)]
+                a = [0.0 if done[j] or d[j] == 0.0 else c[j] / d[j] for j in range(n)]
+                if any(not done[j] and not (d[j] > 0.0) for j in range(n)):
+                    res_info.breakdown = 1
+                if prec is not None:
+                    core.axpby(r, [-x for x in a], mmp, 1.0, r)
+                    z[:] = 0
+                    prec(z, r)
+                    cp = [x.real for x in per_rhs(core.inner_product(r, z), n)]
+                else:
+                    cp = per_rhs(core.axpy_norm2(r, [-x for x in a], mmp, r), n)
+                b = [0.0 if done[j] or c[j] == 0.0 else cp[j] / c[j] for j in range(n)]
+                core.axpby(psi, a, p, 1.0, psi)
+                core.axpby(p, b, p, 1.0, z if prec is not None else r)
+                res = [abs(x) for x in cp]
+                me.history.append(max(res[j] / ssq[j] for j in range(n) if ssq[j] > 0))
+                res_info.iterations = k + 1
+                res_info.residual_sq = [res[j] / ssq[j] if ssq[j] > 0 else 0.0 for j in range(n)]
+                if k + 1 >= me.miniter:
+                    for j in range(n):
+                        if me.eps_abs is not None and res[j] <= me.eps_abs ** 2:
+                            done[j] = True
+                        if res[j] <= rsq[j]:
+                            done[j] = True
+                    if all(done):
+                        res_info.converged = 1
+                        break
+                if res_info.breakdown:
+                    break
+            me.total_iterations += res_info.iterations
+            if me.fail_if_not_converged and not res_info.converged:
+                raise ValueError("FATAL error: CG not converged")
+
+        m = _fermion.matrix_operator(inv, inv_mat=apply)
+        new_dst = getattr(mat, "_new_dst", None)
+        if new_dst is not None:
+            m._new_dst = new_dst
         m.accept_guess = True
         return m
 

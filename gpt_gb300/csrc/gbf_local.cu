@@ -449,22 +449,6 @@ struct SigmaBlocks {
   double2 s[6][2][4];  // [plane][block][2x2]
 };
 
-__device__ __forceinline__ void m3mul(const double2* a, const double2* b, double2* c) {
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double2 s = make_double2(0, 0);
-      for (int k = 0; k < 3; ++k) {
-        double2 q = zmul(a[3 * i + k], b[3 * k + j]);
-        s.x += q.x; s.y += q.y;
-      }
-      c[3 * i + j] = s;
-    }
-}
-__device__ __forceinline__ void m3adj(const double2* a, double2* c) {
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) c[3 * i + j] = zconj(a[3 * j + i]);
-}
-
 struct NatGeo {
   int L[4];
   __device__ long long idx(const int (&x)[4]) const { return x[0] + (long long)L[0] * (x[1] + (long long)L[1] * (x[2] + (long long)L[2] * x[3])); }
@@ -477,21 +461,80 @@ struct NatGeo {
   }
 };
 
-__device__ void vfield(const NatGeo& G, const double2* U, long long V, int mu, int nu, long long y, double2* out) {
+// 3x3 products with operands either in registers or straight from the
+// natural gauge field in memory (no local copies; every index is static so
+// the matrices stay in registers).  op(X) = X or X^dagger.
+template <bool ADJ>
+__device__ __forceinline__ double2 mel(const double2* X, int i, int j) {
+  return ADJ ? zconj(__ldg(X + 3 * j + i)) : __ldg(X + 3 * i + j);
+}
+// out = op(A) op(B), both in memory
+template <bool AA, bool AB>
+__device__ __forceinline__ void mul_mm(const double2* A, const double2* B, double2 (&out)[9]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double2 q = zmul(mel<AA>(A, i, k), mel<AB>(B, k, j));
+        s.x += q.x;
+        s.y += q.y;
+      }
+      out[3 * i + j] = s;
+    }
+}
+// acc += sgn R op(B), R in registers, B in memory
+template <bool AB>
+__device__ __forceinline__ void mul_rm_acc(const double2 (&R)[9], const double2* B, double sgn, double2 (&acc)[9]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double2 q = zmul(R[3 * i + k], mel<AB>(B, k, j));
+        s.x += q.x;
+        s.y += q.y;
+      }
+      acc[3 * i + j].x += sgn * s.x;
+      acc[3 * i + j].y += sgn * s.y;
+    }
+}
+// acc += A R, A in memory, R in registers
+__device__ __forceinline__ void mul_mr_acc(const double2* A, const double2 (&R)[9], double2 (&acc)[9]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double2 q = zmul(mel<false>(A, i, k), R[3 * k + j]);
+        s.x += q.x;
+        s.y += q.y;
+      }
+      acc[3 * i + j].x += s.x;
+      acc[3 * i + j].y += s.y;
+    }
+}
+
+// v(y) = staple_up(y) - staple_down(y) of the (mu, nu) plane:
+//   staple_up(y)   = U_nu(y+mu) U_mu(y+nu)^+ U_nu(y)^+
+//   staple_down(y) = U_nu(z+mu)^+ U_mu(z)^+ U_nu(z),  z = y - nu
+__device__ __forceinline__ void vfield(const NatGeo& G, const double2* U, long long V, int mu, int nu, long long y,
+                                       double2 (&v)[9]) {
   auto L = [&](int m, long long s) { return U + ((size_t)m * V + s) * 9; };
-  double2 p[9], q[9], r9[9], su[9], sd[9];
-  // staple_up(y) = U_nu(y+mu) U_mu(y+nu)^+ U_nu(y)^+
-  m3adj(L(mu, G.shift(y, nu, 1)), p);
-  m3mul(L(nu, G.shift(y, mu, 1)), p, q);
-  m3adj(L(nu, y), p);
-  m3mul(q, p, su);
-  // staple_down(y) = U_nu(z+mu)^+ U_mu(z)^+ U_nu(z), z = y - nu
-  long long z = G.shift(y, nu, -1);
-  m3adj(L(nu, G.shift(z, mu, 1)), p);
-  m3adj(L(mu, z), q);
-  m3mul(p, q, r9);
-  m3mul(r9, L(nu, z), sd);
-  for (int e = 0; e < 9; ++e) out[e] = make_double2(su[e].x - sd[e].x, su[e].y - sd[e].y);
+  double2 t[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) v[e] = make_double2(0.0, 0.0);
+  mul_mm<false, true>(L(nu, G.shift(y, mu, 1)), L(mu, G.shift(y, nu, 1)), t);
+  mul_rm_acc<true>(t, L(nu, y), 1.0, v);
+  const long long z = G.shift(y, nu, -1);
+  mul_mm<true, true>(L(nu, G.shift(z, mu, 1)), L(mu, z), t);
+  mul_rm_acc<false>(t, L(nu, z), -1.0, v);
 }
 
 __device__ bool invert6(double2 (&A)[36], double2 (&I)[36]) {
@@ -526,24 +569,20 @@ __device__ bool invert6(double2 (&A)[36], double2 (&I)[36]) {
   return true;
 }
 
-__device__ void store_clover_block(const double2 (&M)[36], int b, int cb, int Vh, double2* c64, float4* c32) {
-  double re[36];
-  for (int i = 0; i < 6; ++i) re[i] = M[7 * i].x;
-  for (int i = 1; i < 6; ++i)
-    for (int j = 0; j < i; ++j) {
-      re[6 + 2 * tri(i, j)] = M[6 * i + j].x;
-      re[6 + 2 * tri(i, j) + 1] = M[6 * i + j].y;
-    }
-  for (int k = 0; k < 18; ++k) c64[(size_t)(18 * b + k) * Vh + cb] = make_double2(re[2 * k], re[2 * k + 1]);
-  for (int k = 0; k < 9; ++k)
-    c32[(size_t)(9 * b + k) * Vh + cb] = make_float4((float)re[4 * k], (float)re[4 * k + 1], (float)re[4 * k + 2], (float)re[4 * k + 3]);
-}
-
-__global__ void clover_kernel(Geo g, const double2* U, SigmaBlocks sig, double diag, double csw_r, double csw_t, double2* c64,
-                              double2* ci64, float4* c32, float4* ci32, unsigned* err) {
-  const long long xs = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// Clover term of every site, one thread per site: for each plane
+// F_munu = 1/8 (Q - Q^+), Q = U_mu(x) v(x) + v(x-mu) U_mu(x-mu), in registers;
+// -1/2 c_p sigma_munu (x) F_munu is added to the two Hermitian chiral blocks,
+// whose 2 x 36 reals (6 diagonal, 15 complex lower entries each) live in
+// shared memory ([72][blockDim], one column per thread).  Writes the clover
+// blocks in FP64 and FP32 storage; clover_invert_kernel inverts them.
+constexpr int kCloverBlock = 64;
+__global__ void __launch_bounds__(kCloverBlock) clover_kernel(Geo g, const double2* U, SigmaBlocks sig, double diag,
+                                                               double csw_r, double csw_t, double2* c64, float4* c32) {
+  __shared__ double acc[72][kCloverBlock];
+  const int t = threadIdx.x;
+  const long long xs = (long long)blockIdx.x * blockDim.x + t;
   const long long V = 2LL * g.Vh;
-  if (xs >= V) return;
+  if (xs >= V) return;  // no block-wide synchronisation below: each thread owns its column
   NatGeo G;
   for (int m = 0; m < 4; ++m) G.L[m] = g.L[m];
   int x[4];
@@ -551,49 +590,113 @@ __global__ void clover_kernel(Geo g, const double2* U, SigmaBlocks sig, double d
   for (int m = 0; m < 4; ++m) { x[m] = (int)(r % g.L[m]); r /= g.L[m]; }
   const int par = (x[0] + x[1] + x[2] + x[3]) & 1;
   const int cb = cb_index(g, x);
-  double2 blk[2][36];
-  for (int b = 0; b < 2; ++b)
-    for (int e = 0; e < 36; ++e) blk[b][e] = make_double2(e % 7 == 0 ? diag : 0.0, 0.0);
+#pragma unroll
+  for (int e = 0; e < 72; ++e) acc[e][t] = ((e % 36) < 6) ? diag : 0.0;
   int plane = 0;
+#pragma unroll 1
   for (int mu = 0; mu < 4; ++mu)
+#pragma unroll 1
     for (int nu = mu + 1; nu < 4; ++nu, ++plane) {
       const double cp = (nu == 3) ? csw_t : csw_r;
       if (cp == 0.0) continue;
-      double2 v[9], t1[9], t2[9], F[9];
+      double2 v[9], Q[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) Q[e] = make_double2(0.0, 0.0);
       vfield(G, U, V, mu, nu, xs, v);
-      m3mul(U + ((size_t)mu * V + xs) * 9, v, t1);
+      mul_mr_acc(U + ((size_t)mu * V + xs) * 9, v, Q);
       const long long xm = G.shift(xs, mu, -1);
       vfield(G, U, V, mu, nu, xm, v);
-      m3mul(v, U + ((size_t)mu * V + xm) * 9, t2);
-      for (int e = 0; e < 9; ++e) t1[e] = make_double2(t1[e].x + t2[e].x, t1[e].y + t2[e].y);
+      mul_rm_acc<false>(v, U + ((size_t)mu * V + xm) * 9, 1.0, Q);
+      double2 F[9];
+#pragma unroll
       for (int i = 0; i < 3; ++i)
+#pragma unroll
         for (int j = 0; j < 3; ++j) {
-          double2 d = zconj(t1[3 * j + i]);
-          F[3 * i + j] = make_double2(0.125 * (t1[3 * i + j].x - d.x), 0.125 * (t1[3 * i + j].y - d.y));
+          const double2 dq = zconj(Q[3 * j + i]);
+          F[3 * i + j] = make_double2(0.125 * (Q[3 * i + j].x - dq.x), 0.125 * (Q[3 * i + j].y - dq.y));
         }
+#pragma unroll
       for (int b = 0; b < 2; ++b)
+#pragma unroll
         for (int s1 = 0; s1 < 2; ++s1)
+#pragma unroll
           for (int s2 = 0; s2 < 2; ++s2) {
-            double2 sg = sig.s[plane][b][2 * s1 + s2];
-            if (sg.x == 0.0 && sg.y == 0.0) continue;
-            double2 f = make_double2(-0.5 * cp * sg.x, -0.5 * cp * sg.y);
+            const double2 sg = sig.s[plane][b][2 * s1 + s2];
+            const double2 f = make_double2(-0.5 * cp * sg.x, -0.5 * cp * sg.y);
+#pragma unroll
             for (int a = 0; a < 3; ++a)
+#pragma unroll
               for (int c = 0; c < 3; ++c) {
-                double2 q = zmul(f, F[3 * a + c]);
-                double2& e = blk[b][6 * (3 * s1 + a) + (3 * s2 + c)];
-                e.x += q.x;
-                e.y += q.y;
+                const int i = 3 * s1 + a, j = 3 * s2 + c;
+                if (i < j) continue;  // Hermitian: the lower triangle and the diagonal
+                const double2 q = zmul(f, F[3 * a + c]);
+                if (i == j) {
+                  acc[36 * b + i][t] += q.x;
+                } else {
+                  const int tt = tri(i, j);
+                  acc[36 * b + 6 + 2 * tt][t] += q.x;
+                  acc[36 * b + 7 + 2 * tt][t] += q.y;
+                }
               }
           }
     }
   const size_t poff36 = (size_t)par * 36 * g.Vh, poff18 = (size_t)par * 18 * g.Vh;
+#pragma unroll
   for (int b = 0; b < 2; ++b) {
-    store_clover_block(blk[b], b, cb, g.Vh, c64 + poff36, c32 + poff18);
-    double2 A[36], I[36];
-    for (int e = 0; e < 36; ++e) A[e] = blk[b][e];
-    if (!invert6(A, I)) atomic_max_err(err, 1e30);
-    store_clover_block(I, b, cb, g.Vh, ci64 + poff36, ci32 + poff18);
+#pragma unroll
+    for (int k = 0; k < 18; ++k)
+      c64[poff36 + (size_t)(18 * b + k) * g.Vh + cb] = make_double2(acc[36 * b + 2 * k][t], acc[36 * b + 2 * k + 1][t]);
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      c32[poff18 + (size_t)(9 * b + k) * g.Vh + cb] =
+          make_float4((float)acc[36 * b + 4 * k][t], (float)acc[36 * b + 4 * k + 1][t], (float)acc[36 * b + 4 * k + 2][t],
+                      (float)acc[36 * b + 4 * k + 3][t]);
   }
+}
+
+// Inverse of every Hermitian 6x6 clover block, one thread per (site, parity,
+// block), Gauss-Jordan with partial pivoting in FP64 on matrices in shared
+// memory; reads the FP64 clover, writes the FP64 and FP32 inverse.
+constexpr int kInvBlock = 32;
+__global__ void __launch_bounds__(kInvBlock) clover_invert_kernel(int Vh, const double2* c64, double2* ci64, float4* ci32,
+                                                                  unsigned* err) {
+  __shared__ double2 sA[kInvBlock][36], sI[kInvBlock][36];
+  const long long tt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tt >= 4LL * Vh) return;
+  const int cb = (int)(tt % Vh);
+  const int pb = (int)(tt / Vh);
+  const int par = pb >> 1, b = pb & 1;
+  const double2* src = c64 + (size_t)par * 36 * Vh;
+  double re[36];
+#pragma unroll
+  for (int k = 0; k < 18; ++k) {
+    const double2 q = src[(size_t)(18 * b + k) * Vh + cb];
+    re[2 * k] = q.x;
+    re[2 * k + 1] = q.y;
+  }
+  double2(&A)[36] = sA[threadIdx.x];
+  double2(&I)[36] = sI[threadIdx.x];
+  for (int i = 0; i < 6; ++i) A[7 * i] = make_double2(re[i], 0.0);
+  for (int i = 1; i < 6; ++i)
+    for (int j = 0; j < i; ++j) {
+      const double2 v = make_double2(re[6 + 2 * tri(i, j)], re[6 + 2 * tri(i, j) + 1]);
+      A[6 * i + j] = v;
+      A[6 * j + i] = zconj(v);
+    }
+  if (!invert6(A, I)) atomic_max_err(err, 1e30);
+  for (int i = 0; i < 6; ++i) re[i] = I[7 * i].x;
+  for (int i = 1; i < 6; ++i)
+    for (int j = 0; j < i; ++j) {
+      re[6 + 2 * tri(i, j)] = I[6 * i + j].x;
+      re[6 + 2 * tri(i, j) + 1] = I[6 * i + j].y;
+    }
+  double2* d64 = ci64 + (size_t)par * 36 * Vh;
+  float4* d32 = ci32 + (size_t)par * 18 * Vh;
+#pragma unroll
+  for (int k = 0; k < 18; ++k) d64[(size_t)(18 * b + k) * Vh + cb] = make_double2(re[2 * k], re[2 * k + 1]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    d32[(size_t)(9 * b + k) * Vh + cb] = make_float4((float)re[4 * k], (float)re[4 * k + 1], (float)re[4 * k + 2], (float)re[4 * k + 3]);
 }
 
 cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double csw_r, double csw_t, void* c64, void* ci64,
@@ -631,8 +734,12 @@ cudaError_t launch_clover(const Geo& g, const double2* U, double diag, double cs
           for (int s2 = 0; s2 < 2; ++s2) sig.s[plane][b][2 * s1 + s2] = S[4 * (2 * b + s1) + (2 * b + s2)];
     }
   const long long V = 2LL * g.Vh;
-  const unsigned nb = (unsigned)((V + 127) / 128);
-  clover_kernel<<<nb, 128, 0, st>>>(g, U, sig, diag, csw_r, csw_t, (double2*)c64, (double2*)ci64, (float4*)c32, (float4*)ci32, err);
+  clover_kernel<<<(unsigned)((V + kCloverBlock - 1) / kCloverBlock), kCloverBlock, 0, st>>>(
+      g, U, sig, diag, csw_r, csw_t, (double2*)c64, (float4*)c32);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  clover_invert_kernel<<<(unsigned)((2 * V + kInvBlock - 1) / kInvBlock), kInvBlock, 0, st>>>(
+      g.Vh, (const double2*)c64, (double2*)ci64, (float4*)ci32, err);
   return cudaGetLastError();
 }
 
