@@ -1228,6 +1228,9 @@ void cg_results(gbf_op* op, cudaStream_t s, cudaStream_t user, bool device_loop,
   CK(cudaStreamWaitEvent(user, op->ev_out, 0));
   CK(cudaEventSynchronize(op->ev_out));
   const CGState& st = op->hst[0];
+  if (st.kernel_error)
+    throw Fail(GBF_E_CUDA, "a hopping kernel's wait for its bulk copies timed out (code " +
+                               std::to_string(st.kernel_error) + ")");
   if (device_loop) count_launch((unsigned long long)(st.iter > 0 ? st.iter : 1) * kKernelsPerIteration);
   if (res) {
     res->iterations = st.iter;

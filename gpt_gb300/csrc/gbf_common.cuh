@@ -434,6 +434,9 @@ struct CGState {
   int nrhs;
   int breakdown;
   int maxiter;
+  // set by a kernel whose bounded wait for an asynchronous copy ran out
+  // (never expected; the host turns it into an error)
+  int kernel_error;
 };
 
 }  // namespace gbf

@@ -429,6 +429,218 @@ __global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashAr
 }
 
 // ---------------------------------------------------------------------------
+// The hop of hop5_kernel with the neighbour spinors staged in shared memory
+// by 1D bulk copies (cp.async.bulk, global -> shared, completion counted in
+// bytes on an mbarrier), FP32 spinors.  For a tile of S 4D sites and
+// direction d, the N5 inner sites of site j's neighbour are, in each of the
+// 6 16-byte component planes of the FP32 layout, one contiguous run of
+// N5 * 16 bytes; 6 S copies move them into a ring slot laid out
+// [plane][site j][i5], i.e. [plane][thread].  A ring of kRing direction
+// slots keeps kRing - 1 directions in flight while one is computed; thread 0
+// waits for a slot's barrier (bounded) and a block barrier publishes the data
+// and frees the slot used before, which the copy threads then refill.  The
+// ring doubles as the epilogue's shared memory once the 8 directions are
+// done.  A wait that runs out sets st->kernel_error and the block returns
+// (all its threads together, after any copy still in flight has landed).
+// ---------------------------------------------------------------------------
+constexpr int kRing = 4;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// bounded wait for the phase of `parity` to complete: about 1 s of SM clocks
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  const unsigned addr = smem_u32(bar);
+  const long long t0 = clock64();
+  while (true) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > 2000000000LL) return false;
+  }
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__host__ __device__ inline size_t hop5t_ring_bytes(int bd) { return (size_t)kRing * 6 * 16 * bd; }
+
+template <int LK, bool LOOP>
+__global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5t_kernel(const DslashArgs a, int log2S, unsigned links_off16) {
+  using R = float;
+  using V = float2;
+  extern __shared__ __align__(128) double smem_d[];
+  const Geo& g = a.g;
+  if (a.check_done && a.ra.st->all_done) return;
+  const int p = a.out_parity, q = 1 - p;
+  const unsigned t = threadIdx.x, bd = blockDim.x;
+  const unsigned S = 1u << log2S;
+  const unsigned N = (unsigned)g.N, N5 = (unsigned)g.N5;
+  float4* ring = reinterpret_cast<float4*>(smem_d);  // [kRing][6][bd], later the epilogue's region
+  float4* lsm = reinterpret_cast<float4*>(smem_d) + links_off16;  // after max(ring, epilogue)
+  int* nbs = reinterpret_cast<int*>(lsm + S * kHop5LinkStride);
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(nbs + 8 * S);
+  __shared__ int s_ok;
+  if (t == 0) {
+    for (int r = 0; r < kRing; ++r) mbar_init(&full[r], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  unsigned par_bits = 0;  // completion parity of each slot, the same in every thread
+  const unsigned j = g.fN5.div(t);
+  const unsigned i5 = t - j * N5;
+  double red_re = 0, red_im = 0;
+  const long long ntiles = (g.N + bd - 1) / bd;
+  long long tile = blockIdx.x;
+  do {
+    const int cb0 = (int)(tile << log2S);
+    const unsigned s_act = (unsigned)min((long long)S, (long long)g.Vh - cb0);  // sites of this tile
+    for (unsigned idx = t; idx < 8 * S; idx += bd) {
+      const int jj = idx >> 3, d = idx & 7, cbj = cb0 + jj;
+      int ycb = 0;
+      if (cbj < g.Vh) {
+        const Coord c = cb_coords(g, cbj, p);
+        const int mu = d >> 1;
+        int y[4] = {c.x[0], c.x[1], c.x[2], c.x[3]};
+        if ((d & 1) == 0) y[mu] = (y[mu] == g.L[mu] - 1) ? 0 : y[mu] + 1;
+        else y[mu] = (y[mu] == 0) ? g.L[mu] - 1 : y[mu] - 1;
+        ycb = cb_index(g, y);
+      }
+      nbs[idx] = ycb;
+    }
+    __syncthreads();
+    // issue direction d into its slot: thread 0 posts the expected bytes,
+    // threads 0 .. 6 s_act - 1 each copy one plane run of one site
+    auto issue = [&](int d) {
+      const int slot = d % kRing;
+      if (t < 6 * s_act) {
+        if (t == 0) mbar_arrive_expect_tx(&full[slot], 6 * s_act * N5 * 16);
+        const unsigned jj = t / 6, k = t - 6 * jj;
+        const unsigned ycb = (unsigned)nbs[jj * 8 + d];
+        const float4* src = reinterpret_cast<const float4*>(a.in) + (k * N + ycb * N5);
+        float4* dst = ring + ((unsigned)slot * 6 + k) * bd + jj * N5;
+        bulk_g2s(dst, src, N5 * 16, &full[slot]);
+      }
+    };
+    // the ring was last written by the generic proxy (previous epilogue)
+    if (t < 6 * s_act) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+#pragma unroll
+    for (int d = 0; d < kRing; ++d) issue(d);
+    {
+      const float2* L2 = reinterpret_cast<const float2*>(a.links);
+      float* lf = reinterpret_cast<float*>(lsm);
+      for (unsigned idx = t; idx < 72u * S; idx += bd) {
+        const unsigned jj = idx & (S - 1), dk = idx >> log2S;
+        const unsigned d = dk / 9u, k = dk - 9u * d;
+        const int cbj = cb0 + (int)jj;
+        if (cbj >= g.Vh) continue;
+        const int mu = d >> 1;
+        const bool fwd = (d & 1) == 0;
+        const int site = fwd ? cbj : nbs[jj * 8 + d];
+        const int par = fwd ? p : q;
+        float2 v = __ldg(L2 + ((unsigned)((par * 4 + mu) * 9) + k) * (unsigned)g.Vh + (unsigned)site);
+        unsigned kk = k;
+        if (!fwd) {
+          kk = (k % 3u) * 3u + k / 3u;
+          v.y = -v.y;
+        }
+        *reinterpret_cast<float2*>(lf + (jj * kHop5LinkStride + d * 5u) * 4u + 2u * kk) = v;
+      }
+    }
+    const long long n = tile * bd + t;
+    const int cb = cb0 + (int)j;
+    const bool active = cb < g.Vh;
+    V res[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) res[k] = cz<R>();
+    const R sf = (R)a.sgn;
+    const float4* lj = lsm + j * kHop5LinkStride;
+#pragma unroll
+    for (int mu = 0; mu < 4; ++mu) {
+#pragma unroll
+      for (int dir = 0; dir < 2; ++dir) {
+        const int d = 2 * mu + dir;
+        const int slot = d % kRing;
+        if (t == 0) s_ok = mbar_wait_bounded(&full[slot], (par_bits >> slot) & 1u) ? 1 : 0;
+        par_bits ^= 1u << slot;
+        __syncthreads();  // slot d published (and the links); every thread is done with direction d - 1
+        if (!s_ok) {
+          if (t == 0) {
+            atomicExch(&a.ra.st->kernel_error, 1);
+            // let any copy of this block still in flight land before the
+            // block's shared memory is released (about 0.1 s)
+            for (int w = 0; w < 100000; ++w) __nanosleep(1000);
+          }
+          __syncthreads();
+          return;
+        }
+        if (d >= 1 && d - 1 + kRing < 8) issue(d - 1 + kRing);
+        if (active) {
+          const bool fwd = dir == 0;
+          V psi[12];
+          const float4* src = ring + (unsigned)slot * 6 * bd + t;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            const float4 w = src[k * bd];
+            psi[2 * k] = make_float2(w.x, w.y);
+            psi[2 * k + 1] = make_float2(w.z, w.w);
+          }
+          const R s = fwd ? sf : -sf;
+          V h[2][3];
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int col = 0; col < 3; ++col)
+              h[r][col] = coefmadd<R>(gcoef(mu, r), s, psi[3 * gperm(mu, r) + col], psi[3 * r + col]);
+          V u[10];
+#pragma unroll
+          for (int c = 0; c < 5; ++c) {
+            const float4 w = lj[d * 5 + c];
+            u[2 * c] = make_float2(w.x, w.y);
+            u[2 * c + 1] = make_float2(w.z, w.w);
+          }
+          V uh[2][3];
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              V acc = cmul<R>(u[3 * i], h[r][0]);
+              acc = cmadd<R>(acc, u[3 * i + 1], h[r][1]);
+              uh[r][i] = cmadd<R>(acc, u[3 * i + 2], h[r][2]);
+            }
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) res[3 * r + i] = add<R>(res[3 * r + i], uh[r][i]);
+#pragma unroll
+          for (int r = 2; r < 4; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) res[3 * r + i] = coefmadd<R>(gcoef(mu, r), s, uh[gperm(mu, r)][i], res[3 * r + i]);
+        }
+      }
+    }
+    __syncthreads();  // the ring becomes the epilogue's shared memory
+    hop_epilogue<P32, LK>(a, active, n, cb, res, red_re, red_im, smem_d);
+    tile += gridDim.x;
+    __syncthreads();  // the next tile refills the ring and the indices
+  } while (LOOP && tile < ntiles);
+  if (a.red) {
+    double* sm = smem_d + (LK == LOC_SMAT ? (24 * blockDim.x + kSmatWords) * sizeof(R) / sizeof(double) + 1 : 0);
+    block_reduce_finalize(a.ra, red_re, red_im, g.N5, g.Ls, g.nrhs, sm);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host-side launcher
 // ---------------------------------------------------------------------------
 static int sm_count() {
@@ -548,6 +760,36 @@ static cudaError_t launch_hop5(const DslashArgs& a, cudaStream_t st) {
   return loop ? launch_hop5_tl<P, LK, true>(a, bd, st) : launch_hop5_tl<P, LK, false>(a, bd, st);
 }
 
+// the bulk-copy hop: ring (also the epilogue's region), links, indices, barriers
+static size_t hop5t_links_off(int LK, int bd) {
+  const size_t ring = hop5t_ring_bytes(bd), epi = dslash_smem_bytes(P32, LK, bd);
+  return ((ring > epi ? ring : epi) + 15) / 16 * 16;
+}
+static size_t hop5t_smem(int LK, int bd, int S) { return hop5t_links_off(LK, bd) + hop5_extra_smem(S) + kRing * 8; }
+template <int LK, bool LOOP>
+static cudaError_t launch_hop5t_tl(const DslashArgs& a, int bd, cudaStream_t st) {
+  const int S = bd / a.g.N5;
+  int log2S = 0;
+  while ((1 << log2S) < S) ++log2S;
+  const size_t sm = hop5t_smem(LK, bd, S);
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  auto k = hop5t_kernel<LK, LOOP>;
+  const int res = resident_blocks((const void*)k, bd, sm);
+  const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs, res) : ntiles;
+  k<<<(unsigned)nb, bd, sm, st>>>(a, log2S, (unsigned)(hop5t_links_off(LK, bd) / 16));
+  return cudaGetLastError();
+}
+template <int LK>
+static cudaError_t launch_hop5t(const DslashArgs& a, cudaStream_t st) {
+  const int bd = pick_bd(a.bd, a.g.N5);
+  if (bd <= 0) return cudaErrorInvalidValue;
+  const int S = bd / a.g.N5;
+  const long long ntiles = (a.g.N + bd - 1) / bd;
+  const int res = resident_blocks((const void*)hop5t_kernel<LK, true>, bd, hop5t_smem(LK, bd, S));
+  const bool loop = a.red && reduce_grid(ntiles, a.g.nrhs, res) < ntiles;
+  return loop ? launch_hop5t_tl<LK, true>(a, bd, st) : launch_hop5t_tl<LK, false>(a, bd, st);
+}
+
 template <int P, int LS, int LK>
 static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
   const int bd = pick_bd(a.bd, a.g.N5);
@@ -558,8 +800,10 @@ static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
   return loop ? launch_tl<P, LS, LK, true>(a, st) : launch_tl<P, LS, LK, false>(a, st);
 }
 
-// GBF_HOP5=0 in the environment selects the per-thread hop for every field
-// (a switch for comparing the two kernels; results are bitwise equal)
+// GBF_HOP5 in the environment selects the hop of FP32/FP16 fields with an
+// inner extent >= 8: unset or 1 the shared-memory link hop (hop5_kernel),
+// 0 the per-thread hop, 2 the bulk-copy staged hop (hop5t_kernel, FP32);
+// results are bitwise equal, the default is the fastest measured
 static bool hop5_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("GBF_HOP5");
@@ -567,10 +811,20 @@ static bool hop5_enabled() {
   }();
   return on;
 }
+static bool hop5_bulk() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBF_HOP5");
+    return e && e[0] == '2';
+  }();
+  return on;
+}
 
 cudaError_t launch_dslash(int P, int LS, const DslashArgs& a, cudaStream_t st) {
   const int LK = (a.l1.kind == LOC_SMAT || a.l2.kind == LOC_SMAT) ? LOC_SMAT : LOC_CLOVER;
-  // fields with an inner extent of 8 or more: the shared-memory link hop
+  // FP32 fields with an inner extent of 8 or more: the bulk-copy hop when
+  // selected (GBF_HOP5=2), otherwise the shared-memory link hop
+  if (hop5_bulk() && a.g.N5 >= 8 && LS == L32 && P == P32)
+    return LK == LOC_SMAT ? launch_hop5t<LOC_SMAT>(a, st) : launch_hop5t<LOC_CLOVER>(a, st);
   if (hop5_enabled() && a.g.N5 >= 8 && LS == L32 && (P == P32 || P == P16)) {
     if (P == P32) return LK == LOC_SMAT ? launch_hop5<P32, LOC_SMAT>(a, st) : launch_hop5<P32, LOC_CLOVER>(a, st);
     return LK == LOC_SMAT ? launch_hop5<P16, LOC_SMAT>(a, st) : launch_hop5<P16, LOC_CLOVER>(a, st);
