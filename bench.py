@@ -772,6 +772,9 @@ def measure_c5(n_requests, rate=20.0):
     def above(rs):
         return [(r.rid, r.L, r.n_src, max(r.true_residual)) for r in rs if r.true_residual and max(r.true_residual) > 1e-10]
 
+    def errors(rs):
+        return [(r.rid, r.L, r.n_src, r.error[:200]) for r in rs if not r.ok][:4]
+
     # serial baseline: the same stream, one request at a time (max_total 1),
     # plain FP64 eo2_ne CG, drained in arrival order
     serial, swall = serving.Server(ex, budget, method="plain", realtime=False, max_total=1).run(reqs)
@@ -788,16 +791,19 @@ def measure_c5(n_requests, rate=20.0):
            "hbm_budget_bytes": budget, "l2_policy": "per-request working sets; no flush", "parallelism": "replicas"}
     r = {"solves_per_s": s["solves_per_s"], "requests_per_s": s["requests_per_s"],
          "offered_requests_per_s": n_requests / reqs[-1].arrival, "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
-         "failed": s["failed"], "max_true_residual": s["max_true_residual"], "mixed_above_tol": above(res),
+         "failed": s["failed"], "errors": errors(res), "max_true_residual": s["max_true_residual"],
+         "mixed_above_tol": above(res),
          "gpu_launches": int(n1 - n0), "clocks": clk,
          "serial_plain_fp64": {"note": "the same stream served one request at a time (no overlap), plain FP64 CG",
                                "solves_per_s": ss["solves_per_s"], "wall_s": swall, "p50_ms": ss["p50_ms"],
-                               "p99_ms": ss["p99_ms"], "max_true_residual": ss["max_true_residual"],
+                               "p99_ms": ss["p99_ms"], "failed": ss["failed"], "errors": errors(serial),
+                               "max_true_residual": ss["max_true_residual"],
                                "above_tol": above(serial)},
          "speedup_vs_serial_plain": s["solves_per_s"] / ss["solves_per_s"] if ss["solves_per_s"] else None,
          "sustainable_point": {"offered_requests_per_s": offered, "served_requests_per_s": su["requests_per_s"],
                                "solves_per_s": su["solves_per_s"], "p50_ms": su["p50_ms"], "p99_ms": su["p99_ms"],
-                               "failed": su["failed"], "max_true_residual": su["max_true_residual"]}}
+                               "failed": su["failed"], "errors": errors(sres),
+                               "max_true_residual": su["max_true_residual"]}}
     return r, 1000.0 * wall, cfg
 
 

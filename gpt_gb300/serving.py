@@ -123,6 +123,9 @@ class Server:
         self.budget = HBMBudget(hbm_budget_bytes)
         self.caps = caps or default_caps()
         self.max_total = max_total
+        self.max_retries = 3
+        self.retries = collections.Counter()
+        self.requeue = collections.deque()
         self.method = method
         self.realtime = realtime
         self.lock = threading.Condition()
@@ -137,6 +140,17 @@ class Server:
             ok, err = True, ""
         except Exception as e:  # a failed request releases its slot and memory
             fields, ok, err = {}, False, f"{type(e).__name__}: {e}"
+            if "out of memory" in str(e) and self.retries[req.rid] < self.max_retries:
+                # the footprint estimate admitted it, but the device could not
+                # hold it at that moment (memory of other requests not yet
+                # returned): release its share and queue it again
+                self.retries[req.rid] += 1
+                self.budget.release(nbytes)
+                with self.lock:
+                    self.running[req.L] -= 1
+                    self.requeue.append(req)
+                    self.lock.notify_all()
+                return
         end = time.perf_counter()
         res = Result(rid=req.rid, L=req.L, n_src=req.n_src, ok=ok,
                      latency_ms=1000.0 * (end - (t0 + req.arrival)), service_ms=1000.0 * (end - start),
@@ -159,11 +173,17 @@ class Server:
         threads = []
         i = 0
         with self.lock:
-            while i < len(reqs) or waiting:
+            while i < len(reqs) or waiting or self.requeue or sum(self.running.values()) > 0:
                 now = time.perf_counter() - t0
+                while self.requeue:  # out-of-memory retries go first
+                    waiting.appendleft(self.requeue.pop())
                 while i < len(reqs) and (reqs[i].arrival <= now or not self.realtime):
                     waiting.append(reqs[i])
                     i += 1
+                if not waiting and i >= len(reqs):
+                    # only running requests left (one may still come back to retry)
+                    self.lock.wait(timeout=0.05)
+                    continue
                 dispatched = False
                 if waiting:
                     # batch by lattice size: the size class of the oldest waiting request
@@ -230,9 +250,12 @@ def gpu_executor(keep_solution=False, inner_tol=1e-5, iterations_per_graph=0):
             return _run(req, method)
         finally:
             # operator objects sit in reference cycles (their matrix operators
-            # close over them): collect them now so that the request's device
-            # memory returns before the admission of the next one
+            # close over them): collect them now, and hand torch's cached
+            # blocks back to the device, so that the request's device memory
+            # returns before the admission of the next one (the library's own
+            # allocations cannot use torch's cache)
             gc.collect()
+            torch.cuda.empty_cache()
 
     def _run(req, method):
         stream = torch.cuda.Stream()

@@ -13,12 +13,13 @@ from gpt_gb300 import serving
 class FakeExecutor:
     """Sleeps per request and records concurrent device bytes."""
 
-    def __init__(self, fail_rids=()):
+    def __init__(self, fail_rids=(), oom_once=()):
         self.lock = threading.Lock()
         self.live = 0
         self.peak = 0
         self.live_sizes = []
         self.fail_rids = set(fail_rids)
+        self.oom_once = set(oom_once)
         self.order = []
 
     def __call__(self, req, method):
@@ -32,6 +33,10 @@ class FakeExecutor:
             self.live -= nb
         if req.rid in self.fail_rids:
             raise RuntimeError("injected failure")
+        with self.lock:
+            if req.rid in self.oom_once:
+                self.oom_once.discard(req.rid)
+                raise RuntimeError("cudaMalloc of 1 bytes failed: out of memory")
         return {"true_residual": [1e-11] * req.n_src, "checksum": [float(req.rid)] * req.n_src}
 
 
@@ -74,6 +79,18 @@ def test_failed_request_releases_memory_and_others_finish():
     assert sorted(r.rid for r in bad) == [3, 11] and "injected failure" in bad[0].error
     assert srv.budget.used == 0
     assert serving.summarize(res, wall)["failed"] == 2
+
+
+def test_out_of_memory_is_retried_not_failed():
+    # a request admitted by its footprint estimate may still meet a device
+    # that cannot hold it yet: it goes back to the queue and completes later
+    reqs = serving.poisson_stream(16, 5000.0, seed=11)
+    ex = FakeExecutor(oom_once={2, 9})
+    srv = serving.Server(ex, 10 * serving.footprint_bytes(32, 12), realtime=False)
+    res, wall = srv.run(reqs)
+    assert len(res) == 16 and all(r.ok for r in res)
+    assert srv.retries[2] == 1 and srv.retries[9] == 1
+    assert srv.budget.used == 0 and sum(srv.running.values()) == 0
 
 
 def test_batching_dispatches_same_size_together():
