@@ -1665,7 +1665,7 @@ void apply_ne(gbf_op* op, cudaStream_t s, const void* in, void* out) {
 zmat gram(gbf_op* op, cudaStream_t s, const void* A, const void* B) {
   const int k = op->g.nrhs;
   CK(launch_gram(op->prec, op->g, A, B, op->blk_partial, op->blk_max_blocks, op->counter, op->blk_dev, s));
-  count_launch();
+  count_launch(gram_launches(op->prec, op->g));
   CK(cudaMemcpyAsync(op->blk_host, op->blk_dev, (size_t)k * k * sizeof(double2), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   zmat m((size_t)k * k);

@@ -30,6 +30,24 @@ __device__ __forceinline__ void tile_load(const R* tile, int bd, int t, cplx<R> 
 #pragma unroll
   for (int c = 0; c < 12; ++c) v[c] = mk<R>(tile[(2 * c) * bd + t], tile[(2 * c + 1) * bd + t]);
 }
+// FP32: two complex components per 16-byte word ([6][bd] float4), read back
+// with 6 vector loads instead of 24 scalar ones
+template <>
+__device__ __forceinline__ void tile_store<float>(float* tile, int bd, int t, const float2 (&v)[12]) {
+  float4* q = reinterpret_cast<float4*>(tile);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) q[c * bd + t] = make_float4(v[2 * c].x, v[2 * c].y, v[2 * c + 1].x, v[2 * c + 1].y);
+}
+template <>
+__device__ __forceinline__ void tile_load<float>(const float* tile, int bd, int t, float2 (&v)[12]) {
+  const float4* q = reinterpret_cast<const float4*>(tile);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const float4 w = q[c * bd + t];
+    v[2 * c] = make_float2(w.x, w.y);
+    v[2 * c + 1] = make_float2(w.z, w.w);
+  }
+}
 
 // conj(a) . b of one site in the arithmetic precision R
 template <typename R>
@@ -128,6 +146,228 @@ __global__ void __launch_bounds__(256) gram_kernel(const Geo g, const void* A, c
     if (lane == 0) out[q] = make_double2(re, im);
   }
   if (t == 0) *counter = 0u;
+}
+
+// The same Gram matrix for FP32 / FP16 fields, register-tiled.  A tile of
+// bd 5D sites (S 4D sites x Ls x k vectors) is staged in shared memory as
+// [component c][row r = (site, s)][vector i] for A and B.  Threads form
+// groups of 16, a 4 x 4 grid: thread (ti, tj) owns the T x T block of
+// entries i in [T ti, T ti + T), j in [T tj, T tj + T) (T = ceil(k / 4)) and,
+// for the (c, r) pairs of its group, reads T values of A and T of B and does
+// 4 T^2 fused multiply-adds -- each shared-memory value feeds 2 T complex
+// products instead of one.  Per tile the products are summed in FP32, then
+// added to FP64 accumulators; the block sums its groups in a fixed order and
+// the last block the [block][k*k] partials in block order (deterministic).
+template <int P, int T>
+__global__ void __launch_bounds__(256) gram_tiled_kernel(const Geo g, const void* A, const void* B, double2* partial) {
+  using V = float2;
+  extern __shared__ __align__(16) double sm_d[];
+  const int k = g.nrhs, t = threadIdx.x, bd = blockDim.x;
+  const int Ls = g.Ls, N5 = g.N5, R = (bd / N5) * Ls;  // rows per tile
+  V* sA = reinterpret_cast<V*>(sm_d);                  // [12][R][k]
+  V* sB = sA + 12 * R * k;
+  const int grp = t >> 4, l16 = t & 15, ti = l16 >> 2, tj = l16 & 3, G = bd >> 4;
+  // staging position of this thread's site: n_local = jsite N5 + iv Ls + s
+  const int jsite = t / N5, i5 = t - jsite * N5, iv = i5 / Ls, s = i5 - iv * Ls;
+  const int row = jsite * Ls + s;
+  double dre[T][T], dim[T][T];
+#pragma unroll
+  for (int x = 0; x < T; ++x)
+#pragma unroll
+    for (int y = 0; y < T; ++y) dre[x][y] = dim[x][y] = 0.0;
+  const long long ntiles = (g.N + bd - 1) / bd;
+  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
+    const long long n = tl * bd + t;
+    V a[12], b[12];
+    if (n < g.N) {
+      load_spinor<P>(A, g.N, n, a);
+      load_spinor<P>(B, g.N, n, b);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) a[c] = b[c] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < 12; ++c) {
+      sA[(c * R + row) * k + iv] = a[c];
+      sB[(c * R + row) * k + iv] = b[c];
+    }
+    __syncthreads();
+    float fre[T][T], fim[T][T];
+#pragma unroll
+    for (int x = 0; x < T; ++x)
+#pragma unroll
+      for (int y = 0; y < T; ++y) fre[x][y] = fim[x][y] = 0.f;
+    for (int pq = grp; pq < 12 * R; pq += G) {
+      const V* pa = sA + pq * k + T * ti;  // pq = c R + r
+      const V* pb = sB + pq * k + T * tj;
+      V av[T], bv[T];
+#pragma unroll
+      for (int x = 0; x < T; ++x) {
+        av[x] = (T * ti + x < k) ? pa[x] : make_float2(0.f, 0.f);
+        bv[x] = (T * tj + x < k) ? pb[x] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int x = 0; x < T; ++x)
+#pragma unroll
+        for (int y = 0; y < T; ++y) {  // conj(a) b
+          fre[x][y] = fmaf(av[x].x, bv[y].x, fre[x][y]);
+          fre[x][y] = fmaf(av[x].y, bv[y].y, fre[x][y]);
+          fim[x][y] = fmaf(av[x].x, bv[y].y, fim[x][y]);
+          fim[x][y] = fmaf(-av[x].y, bv[y].x, fim[x][y]);
+        }
+    }
+#pragma unroll
+    for (int x = 0; x < T; ++x)
+#pragma unroll
+      for (int y = 0; y < T; ++y) {
+        dre[x][y] += (double)fre[x][y];
+        dim[x][y] += (double)fim[x][y];
+      }
+    __syncthreads();
+  }
+  // block sum over the groups, fixed order ([group][k*k] doubles in the tile region)
+  double2* red = reinterpret_cast<double2*>(sm_d);
+#pragma unroll
+  for (int x = 0; x < T; ++x)
+#pragma unroll
+    for (int y = 0; y < T; ++y) {
+      const int i = T * ti + x, j = T * tj + y;
+      if (i < k && j < k) red[grp * k * k + i * k + j] = make_double2(dre[x][y], dim[x][y]);
+    }
+  __syncthreads();
+  for (int q = t; q < k * k; q += bd) {
+    double re = 0.0, im = 0.0;
+    for (int gg = 0; gg < G; ++gg) {
+      const double2 v = red[gg * k * k + q];
+      re += v.x;
+      im += v.y;
+    }
+    partial[(size_t)blockIdx.x * k * k + q] = make_double2(re, im);
+  }
+}
+
+// The FP32 Gram with the tiles double-buffered: while a tile is reduced the
+// next one streams into the other buffer with cp.async 16-byte copies (no
+// registers held for staging, the loads of one tile overlap the arithmetic of
+// the previous one).  Layout per buffer and field: [component pair cp][row r]
+// [vector i] of float4 (components 2 cp and 2 cp + 1 of one site, exactly
+// one 16-byte word of the field's FP32 layout); each (cp, r) pair gives
+// 8 T^2 fused multiply-adds for 2 T vector loads.  Summation as in
+// gram_tiled_kernel (FP32 within a tile, FP64 across tiles, fixed orders).
+__device__ __forceinline__ void cpa16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int T>
+__global__ void __launch_bounds__(256) gram_async_kernel(const Geo g, const void* A, const void* B, double2* partial) {
+  extern __shared__ __align__(16) double sm_d[];
+  const int k = g.nrhs, t = threadIdx.x, bd = blockDim.x;
+  const int Ls = g.Ls, N5 = g.N5, R = (bd / N5) * Ls;
+  float4* buf = reinterpret_cast<float4*>(sm_d);  // [2 buffers][A, B][6][R][k]
+  const int fld = 6 * R * k;                      // float4 per field and buffer (= 6 bd)
+  const int grp = t >> 4, l16 = t & 15, ti = l16 >> 2, tj = l16 & 3, G = bd >> 4;
+  const int jsite = t / N5, i5 = t - jsite * N5, iv = i5 / Ls, s = i5 - iv * Ls;
+  const int row = jsite * Ls + s;
+  const float4* gA = reinterpret_cast<const float4*>(A);
+  const float4* gB = reinterpret_cast<const float4*>(B);
+  const unsigned N = (unsigned)g.N;
+  double dre[T][T], dim[T][T];
+#pragma unroll
+  for (int x = 0; x < T; ++x)
+#pragma unroll
+    for (int y = 0; y < T; ++y) dre[x][y] = dim[x][y] = 0.0;
+  const long long ntiles = (g.N + bd - 1) / bd;
+  // stage tile tl into buffer b (absent sites: zeros written by the thread)
+  auto stage = [&](long long tl, int b) {
+    const long long n = tl * bd + t;
+    float4* dA = buf + (size_t)b * 2 * fld;
+    float4* dB = dA + fld;
+#pragma unroll
+    for (int cp = 0; cp < 6; ++cp) {
+      const int o = (cp * R + row) * k + iv;
+      if (n < g.N) {
+        cpa16(dA + o, gA + ((unsigned)n + (unsigned)cp * N));
+        cpa16(dB + o, gB + ((unsigned)n + (unsigned)cp * N));
+      } else {
+        dA[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        dB[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    cpa_commit();
+  };
+  long long tl = blockIdx.x;
+  int b = 0;
+  if (tl < ntiles) stage(tl, 0);
+  for (; tl < ntiles; tl += gridDim.x, b ^= 1) {
+    const long long nxt = tl + gridDim.x;
+    if (nxt < ntiles) {
+      stage(nxt, b ^ 1);
+      cpa_wait1();  // this thread's copies of the current tile have landed
+    } else {
+      cpa_wait0();
+    }
+    __syncthreads();  // every thread's copies of the current tile
+    const float4* sA = buf + (size_t)b * 2 * fld;
+    const float4* sB = sA + fld;
+    float fre[T][T], fim[T][T];
+#pragma unroll
+    for (int x = 0; x < T; ++x)
+#pragma unroll
+      for (int y = 0; y < T; ++y) fre[x][y] = fim[x][y] = 0.f;
+    for (int pq = grp; pq < 6 * R; pq += G) {  // pq = cp R + r
+      const float4* pa = sA + pq * k + T * ti;
+      const float4* pb = sB + pq * k + T * tj;
+      float4 av[T], bv[T];
+#pragma unroll
+      for (int x = 0; x < T; ++x) {
+        av[x] = (T * ti + x < k) ? pa[x] : make_float4(0.f, 0.f, 0.f, 0.f);
+        bv[x] = (T * tj + x < k) ? pb[x] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int x = 0; x < T; ++x)
+#pragma unroll
+        for (int y = 0; y < T; ++y) {  // conj(a) b over the two components
+          fre[x][y] = fmaf(av[x].x, bv[y].x, fre[x][y]);
+          fre[x][y] = fmaf(av[x].y, bv[y].y, fre[x][y]);
+          fre[x][y] = fmaf(av[x].z, bv[y].z, fre[x][y]);
+          fre[x][y] = fmaf(av[x].w, bv[y].w, fre[x][y]);
+          fim[x][y] = fmaf(av[x].x, bv[y].y, fim[x][y]);
+          fim[x][y] = fmaf(-av[x].y, bv[y].x, fim[x][y]);
+          fim[x][y] = fmaf(av[x].z, bv[y].w, fim[x][y]);
+          fim[x][y] = fmaf(-av[x].w, bv[y].z, fim[x][y]);
+        }
+    }
+#pragma unroll
+    for (int x = 0; x < T; ++x)
+#pragma unroll
+      for (int y = 0; y < T; ++y) {
+        dre[x][y] += (double)fre[x][y];
+        dim[x][y] += (double)fim[x][y];
+      }
+    __syncthreads();  // the buffer is refilled two tiles on
+  }
+  double2* red = reinterpret_cast<double2*>(sm_d);
+#pragma unroll
+  for (int x = 0; x < T; ++x)
+#pragma unroll
+    for (int y = 0; y < T; ++y) {
+      const int i = T * ti + x, j = T * tj + y;
+      if (i < k && j < k) red[grp * k * k + i * k + j] = make_double2(dre[x][y], dim[x][y]);
+    }
+  __syncthreads();
+  for (int q = t; q < k * k; q += bd) {
+    double re = 0.0, im = 0.0;
+    for (int gg = 0; gg < G; ++gg) {
+      const double2 v = red[gg * k * k + q];
+      re += v.x;
+      im += v.y;
+    }
+    partial[(size_t)blockIdx.x * k * k + q] = make_double2(re, im);
+  }
 }
 
 // out_i = beta Y_i + sum_j X_j W[j][i]  (W: k x k complex, row j = coefficients
@@ -260,6 +500,96 @@ __global__ void __launch_bounds__(256) lincomb2_kernel(const Geo g, void* out1, 
   }
 }
 
+// lincomb2_kernel for FP32 with the X1 and X2 tiles double-buffered by
+// cp.async (layout [component pair][thread] float4, one 16-byte word per
+// copy): the next tile's copies overlap this tile's combinations.
+__global__ void __launch_bounds__(256) lincomb2_async_kernel(const Geo g, void* out1, const void* Y1, double b1,
+                                                             const void* X1, const double2* W1, void* out2,
+                                                             const void* Y2, double b2, double c, const void* X2,
+                                                             const double2* W2) {
+  using V = float2;
+  extern __shared__ __align__(16) double sm[];
+  float4* buf = reinterpret_cast<float4*>(sm);  // [2 buffers][X1, X2][6][bd]
+  const int k = g.nrhs, t = threadIdx.x, bd = blockDim.x;
+  const int i = (int)g.fLs.div((unsigned)(t % g.N5));
+  const unsigned N = (unsigned)g.N;
+  const float4* gx1 = reinterpret_cast<const float4*>(X1);
+  const float4* gx2 = reinterpret_cast<const float4*>(X2);
+  const long long ntiles = (g.N + bd - 1) / bd;
+  auto stage = [&](long long tl, int b) {
+    const long long n = tl * bd + t;
+    float4* d1 = buf + (size_t)b * 12 * bd;
+    float4* d2 = d1 + 6 * bd;
+    if (n < g.N) {
+#pragma unroll
+      for (int cp = 0; cp < 6; ++cp) {
+        cpa16(d1 + cp * bd + t, gx1 + ((unsigned)n + (unsigned)cp * N));
+        cpa16(d2 + cp * bd + t, gx2 + ((unsigned)n + (unsigned)cp * N));
+      }
+    }
+    cpa_commit();
+  };
+  long long tl = blockIdx.x;
+  int b = 0;
+  if (tl < ntiles) stage(tl, 0);
+  for (; tl < ntiles; tl += gridDim.x, b ^= 1) {
+    const long long nxt = tl + gridDim.x;
+    if (nxt < ntiles) stage(nxt, b ^ 1);
+    const long long n = tl * bd + t;
+    // this site's own Y1 and Y2, loaded before the wait so that their latency
+    // overlaps it
+    V acc[12], y2v[12];
+    if (n < g.N) {
+      if (Y1) load_spinor<P32>(Y1, g.N, n, acc);
+      if (Y2) load_spinor<P32>(Y2, g.N, n, y2v);
+    }
+    if (nxt < ntiles) cpa_wait1();
+    else cpa_wait0();
+    __syncthreads();
+    if (n < g.N) {
+      const float* tile1 = reinterpret_cast<const float*>(buf + (size_t)b * 12 * bd);
+      const float* tile2 = tile1 + 24 * bd;
+      if (Y1) {
+        const float bb = (float)b1;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc[q] = scl<float>(bb, acc[q]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc[q] = cz<float>();
+      }
+      for (int j = 0; j < k; ++j) {
+        V x[12];
+        tile_load<float>(tile1, bd, t + (j - i) * g.Ls, x);
+        const double2 w = __ldg(W1 + j * k + i);
+        const V wc = make_float2((float)w.x, (float)w.y);
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc[q] = cmadd<float>(acc[q], wc, x[q]);
+      }
+      store_spinor<P32>(out1, g.N, n, acc);
+      V acc2[12];
+      const float cc = (float)c;
+      if (Y2) {
+        const float bb = (float)b2;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc2[q] = make_float2(fmaf(cc, acc[q].x, bb * y2v[q].x), fmaf(cc, acc[q].y, bb * y2v[q].y));
+      } else {
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc2[q] = scl<float>(cc, acc[q]);
+      }
+      for (int j = 0; j < k; ++j) {
+        V x[12];
+        tile_load<float>(tile2, bd, t + (j - i) * g.Ls, x);
+        const double2 w = __ldg(W2 + j * k + i);
+        const V wc = make_float2((float)w.x, (float)w.y);
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc2[q] = cmadd<float>(acc2[q], wc, x[q]);
+      }
+      store_spinor<P32>(out2, g.N, n, acc2);
+    }
+    __syncthreads();
+  }
+}
+
 static size_t tile_bytes(int P, int bd) { return (size_t)24 * bd * ((P == P64 || P == PDD) ? 8 : 4); }
 
 cudaError_t launch_lincomb2(int P, const Geo& g, void* out1, const void* Y1, double b1, const void* X1, const double2* W1,
@@ -272,6 +602,13 @@ cudaError_t launch_lincomb2(int P, const Geo& g, void* out1, const void* Y1, dou
                 : P == P16 ? (const void*)lincomb2_kernel<P16>
                 : P == PDD ? (const void*)lincomb2_kernel<PDD> : nullptr;
   if (!k) return cudaErrorInvalidValue;
+  if (P == P32) {
+    const size_t sma = (size_t)2 * 12 * bd * sizeof(float4);
+    const long long nba =
+        reduce_grid((g.N + bd - 1) / bd, g.nrhs, resident_blocks((const void*)lincomb2_async_kernel, bd, sma));
+    lincomb2_async_kernel<<<(unsigned)nba, bd, sma, st>>>(g, out1, Y1, b1, X1, W1, out2, Y2, b2, c, X2, W2);
+    return cudaGetLastError();
+  }
   const size_t sm = 2 * tile_bytes(P, bd);
   const long long nb = reduce_grid((g.N + bd - 1) / bd, g.nrhs, resident_blocks(k, bd, sm));
 #define GBF_L2(PP) lincomb2_kernel<PP><<<(unsigned)nb, bd, sm, st>>>(g, out1, Y1, b1, X1, W1, out2, Y2, b2, c, X2, W2)
@@ -295,10 +632,88 @@ static cudaError_t launch_gram_t(const Geo& g, const void* A, const void* B, dou
   return cudaGetLastError();
 }
 
+// Sum of the [block][k*k] Gram partials: one block of 256 threads per entry
+// q, its threads take blocks b = t, t + 256, ... in order and a fixed
+// shuffle tree adds them (deterministic; many blocks share the work instead
+// of one last block walking every entry).
+__global__ void __launch_bounds__(256) gram_finalize_kernel(const double2* partial, int nblocks, int kk, double2* out) {
+  __shared__ double sm[64];
+  const int q = blockIdx.x, t = threadIdx.x;
+  double re = 0.0, im = 0.0;
+  for (int b = t; b < nblocks; b += blockDim.x) {
+    const double2 v = partial[(size_t)b * kk + q];
+    re += v.x;
+    im += v.y;
+  }
+  const double2 r = block_sum_shfl(re, im, sm);
+  if (t == 0) out[q] = r;
+}
+
+template <int P, int T>
+static cudaError_t launch_gram_tiled(const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
+                                     unsigned* counter, double2* out, int bd, cudaStream_t st) {
+  // staged tiles: 2 x 12 x bd complex floats; the group sums reuse them
+  size_t sm = (size_t)2 * 12 * bd * sizeof(float2);
+  const size_t red = (size_t)(bd / 16) * g.nrhs * g.nrhs * sizeof(double2);
+  if (red > sm) sm = red;
+  auto k = gram_tiled_kernel<P, T>;
+  const int res = resident_blocks((const void*)k, bd, sm);
+  long long nb = reduce_grid((g.N + bd - 1) / bd, 1, res);
+  if (nb > max_blocks) nb = max_blocks;
+  (void)counter;
+  k<<<(unsigned)nb, bd, sm, st>>>(g, A, B, partial);
+  gram_finalize_kernel<<<(unsigned)(g.nrhs * g.nrhs), 256, 0, st>>>(partial, (int)nb, g.nrhs * g.nrhs, out);
+  return cudaGetLastError();
+}
+
+template <int T>
+static cudaError_t launch_gram_async(const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
+                                     unsigned* counter, double2* out, int bd, cudaStream_t st) {
+  // two buffers of the A and B tiles (2 x 2 x 6 bd float4); the group sums reuse them
+  size_t sm = (size_t)2 * 2 * 6 * bd * sizeof(float4);
+  const size_t red = (size_t)(bd / 16) * g.nrhs * g.nrhs * sizeof(double2);
+  if (red > sm) sm = red;
+  auto k = gram_async_kernel<T>;
+  const int res = resident_blocks((const void*)k, bd, sm);
+  long long nb = reduce_grid((g.N + bd - 1) / bd, 1, res);
+  if (nb > max_blocks) nb = max_blocks;
+  (void)counter;
+  k<<<(unsigned)nb, bd, sm, st>>>(g, A, B, partial);
+  gram_finalize_kernel<<<(unsigned)(g.nrhs * g.nrhs), 256, 0, st>>>(partial, (int)nb, g.nrhs * g.nrhs, out);
+  return cudaGetLastError();
+}
+
+template <int P>
+static cudaError_t launch_gram_tiled_k(const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
+                                       unsigned* counter, double2* out, int bd, cudaStream_t st) {
+  const int T = (g.nrhs + 3) / 4;
+  if (T == 1) return launch_gram_tiled<P, 1>(g, A, B, partial, max_blocks, counter, out, bd, st);
+  if (T == 2) return launch_gram_tiled<P, 2>(g, A, B, partial, max_blocks, counter, out, bd, st);
+  if (T == 3) return launch_gram_tiled<P, 3>(g, A, B, partial, max_blocks, counter, out, bd, st);
+  return launch_gram_tiled<P, 4>(g, A, B, partial, max_blocks, counter, out, bd, st);
+}
+
+// kernels one launch_gram issues (the FP32 / FP16 path adds the finalisation)
+int gram_launches(int P, const Geo& g) {
+  const int bd = block_size_for(g.N5, LOC_NONE);
+  return ((P == P32 || P == P16) && bd > 0 && bd % 16 == 0) ? 2 : 1;
+}
+
 cudaError_t launch_gram(int P, const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
                         unsigned* counter, double2* out, cudaStream_t st) {
   const int bd = block_size_for(g.N5, LOC_NONE);
   if (bd <= 0 || g.nrhs > kMaxRhs) return cudaErrorInvalidValue;
+  // FP32 / FP16: the register-tiled kernel (groups of 16 threads)
+  if ((P == P32 || P == P16) && bd % 16 == 0) {
+    if (P == P32) {
+      const int T = (g.nrhs + 3) / 4;
+      if (T == 1) return launch_gram_async<1>(g, A, B, partial, max_blocks, counter, out, bd, st);
+      if (T == 2) return launch_gram_async<2>(g, A, B, partial, max_blocks, counter, out, bd, st);
+      if (T == 3) return launch_gram_async<3>(g, A, B, partial, max_blocks, counter, out, bd, st);
+      return launch_gram_async<4>(g, A, B, partial, max_blocks, counter, out, bd, st);
+    }
+    return launch_gram_tiled_k<P16>(g, A, B, partial, max_blocks, counter, out, bd, st);
+  }
   if (P == P64) return launch_gram_t<P64>(g, A, B, partial, max_blocks, counter, out, bd, st);
   if (P == P32) return launch_gram_t<P32>(g, A, B, partial, max_blocks, counter, out, bd, st);
   if (P == P16) return launch_gram_t<P16>(g, A, B, partial, max_blocks, counter, out, bd, st);

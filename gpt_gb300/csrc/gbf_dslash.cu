@@ -664,7 +664,9 @@ int resident_blocks(const void* kernel, int bd, size_t smem) {
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  if (smem > 48 * 1024 && smem > limit[kernel]) {
+  // (raised for every size above the current limit: a kernel's static shared
+  // memory counts against the same 48 KB default as the dynamic request)
+  if (smem > limit[kernel]) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     limit[kernel] = smem;
   }

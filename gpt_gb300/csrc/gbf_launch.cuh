@@ -112,6 +112,7 @@ cudaError_t launch_split_dd(const void* src64, void* dst, long long n_complex, c
 // on entry, restored), and out_i = beta Y_i + sum_j X_j W[j k + i]
 cudaError_t launch_gram(int P, const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
                         unsigned* counter, double2* out, cudaStream_t st);
+int gram_launches(int P, const Geo& g);
 cudaError_t launch_lincomb(int P, const Geo& g, void* out, const void* Y, double beta, const void* X, const double2* W,
                            cudaStream_t st);
 // multi-shift CG update over the active shifts: x_j += a_j p_j ; p_j = b_j p_j + g_j r

@@ -87,10 +87,15 @@ def test_block_cg_needs_no_more_iterations_than_packed_cg():
     assert bcg.last.iterations <= cg.last.iterations
 
 
-def test_block_cg_single_precision_inner_in_defect_correction():
-    dims = [4, 4, 4, 8]
-    nrhs = 4
-    op, ref = _ops("wilson_clover", WC, dims, nrhs, g.double)
+@pytest.mark.parametrize("kind,params,nrhs,dims", [
+    ("wilson_clover", WC, 4, [4, 4, 4, 8]),
+    # k = 12 packed sources in 5D (the 12-source propagator's shape): the
+    # register-tiled FP32 Gram with 3 x 3 entry blocks per thread
+    ("mobius", dict(MOB, Ls=4), 12, [4, 4, 4, 8]),
+    ("wilson_clover", WC, 7, [4, 4, 4, 8]),
+])
+def test_block_cg_single_precision_inner_in_defect_correction(kind, params, nrhs, dims):
+    op, ref = _ops(kind, params, dims, nrhs, g.double)
     shape = op.F_lattice()[:].shape[1:]
     srcs = [_rand(shape, 90 + k) for k in range(nrhs)]
     B = op.F_lattice()
