@@ -641,6 +641,228 @@ __global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5t_kernel(const DslashA
 }
 
 // ---------------------------------------------------------------------------
+// The double-float hop with two threads per 5D site (one right-hand side,
+// per-thread epilogue).  Thread r = 0, 1 of a site projects the half spinor
+// h_r = psi_r + s coef psi_perm(r) of every direction, multiplies it by the
+// link and accumulates it into upper spin r and into the lower spin that
+// takes h_r in that direction; its accumulators (upper spin r, both lower
+// spins: 9 double-float complex numbers) live in shared memory.  After the 8
+// directions the pair exchanges partial sums through shared memory and
+// thread r owns chiral half r (spins 2r, 2r+1; the clover term is
+// block-diagonal in the chiral basis) for the epilogue: its 6x6 clover or
+// twisted-mass block, the X term, the store and its share of the
+// reduction.  Against dslash_kernel<PDD> this halves the registers a thread
+// needs (same arithmetic per site), so about twice the warps are resident to
+// cover the latency of the double-float operation chains.  The lower spins
+// are summed as thread 0's directions plus thread 1's (a fixed order).
+// ---------------------------------------------------------------------------
+#ifndef GBF_DD2_MINB
+#define GBF_DD2_MINB 3
+#endif
+constexpr int kDD2Acc = 9;  // accumulators per thread: upper spin r (3), lower spins 2, 3 (6)
+
+__device__ __forceinline__ cplx<dd> f4dd(const float4 q) { return mk<dd>(dd(q.x, q.z), dd(q.y, q.w)); }
+__device__ __forceinline__ float4 ddf4(cplx<dd> v) {
+  nrm<dd>(v);
+  return make_float4(v.x.h, v.y.h, v.x.l, v.y.l);
+}
+
+// one chiral 6x6 block b of the double-float clover storage applied to w
+__device__ __forceinline__ void clover_block_dd(const void* base, int Vh, int cb, int b, ddc (&w)[6]) {
+  const float4* pb = reinterpret_cast<const float4*>(base) + cb + 18u * (unsigned)b * (unsigned)Vh;
+  ddc o[6];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float4 q = __ldg(pb + (unsigned)k * (unsigned)Vh);
+    o[2 * k] = scl<dd>(dd(q.x, q.z), w[2 * k]);
+    o[2 * k + 1] = scl<dd>(dd(q.y, q.w), w[2 * k + 1]);
+  }
+#pragma unroll
+  for (int i = 1; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < i; ++j) {
+      const float4 q = __ldg(pb + (unsigned)(3 + tri(i, j)) * (unsigned)Vh);
+      const ddc cij = mk<dd>(dd(q.x, q.z), dd(q.y, q.w));
+      o[i] = cmadd<dd>(o[i], cij, w[j]);
+      o[j] = cmaddc<dd>(o[j], cij, w[i]);
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) w[i] = o[i];
+}
+// site-local op restricted to chiral half b
+__device__ __forceinline__ void local_half_dd(const LocalOp& l, int Vh, int parity, int cb, int b, ddc (&w)[6]) {
+  if (l.kind == LOC_CLOVER) {
+    clover_block_dd(l.clov[parity], Vh, cb, b, w);
+  } else if (l.kind == LOC_TWIST) {
+    const ddc z = mk<dd>(dd(l.z[2 * b]), dd(l.z[2 * b + 1]));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      nrm<dd>(w[k]);
+      w[k] = cmul<dd>(z, w[k]);
+    }
+  } else if (l.kind == LOC_SCALAR) {
+    const dd sc(l.scalar);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      nrm<dd>(w[k]);
+      w[k] = scl<dd>(sc, w[k]);
+    }
+  }
+}
+
+template <bool LOOP>
+__global__ void __launch_bounds__(256, GBF_DD2_MINB) dslash_dd2_kernel(const DslashArgs a) {
+  extern __shared__ __align__(16) double smem_d[];
+  const Geo& g = a.g;
+  if (a.check_done && a.ra.st->all_done) return;
+  const int p = a.out_parity, q = 1 - p;
+  const unsigned t = threadIdx.x, bs = blockDim.x;
+  const unsigned r = t & 1u;
+  const unsigned sites = bs >> 1;
+  float4* acc = reinterpret_cast<float4*>(smem_d) + t;  // [kDD2Acc][bs]
+  const unsigned N = (unsigned)g.N;
+  const float4* sp = reinterpret_cast<const float4*>(a.in);
+  const float4* lk = reinterpret_cast<const float4*>(a.links);
+  double red_re = 0, red_im = 0;
+  const long long ntiles = (g.N + sites - 1) / sites;
+  long long tile = blockIdx.x;
+  do {
+    const long long n = tile * sites + (t >> 1);
+    const bool active = n < g.N;
+    int cb = 0;
+    if (active) {
+      cb = (int)g.fN5.div((unsigned)n);
+      const unsigned i5 = (unsigned)n - (unsigned)cb * (unsigned)g.N5;
+      const Coord c = cb_coords(g, cb, p);
+#pragma unroll
+      for (int k = 0; k < kDD2Acc; ++k) acc[k * bs] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+      for (int d = 0; d < 8; ++d) {
+        const int mu = d >> 1;
+        const bool fwd = (d & 1) == 0;
+        int y[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const int xm = c.x[m], Lm = g.L[m];
+          y[m] = (m != mu) ? xm : fwd ? (xm == Lm - 1 ? 0 : xm + 1) : (xm == 0 ? Lm - 1 : xm - 1);
+        }
+        const int ycb = cb_index(g, y);
+        const unsigned site = (unsigned)ycb * (unsigned)g.N5 + i5;
+        const float s = fwd ? a.sgn : -a.sgn;
+        const int pr = gperm(mu, (int)r), cr = gcoef(mu, (int)r);
+        cplx<dd> h[3];
+#pragma unroll
+        for (int col = 0; col < 3; ++col) {
+          const cplx<dd> up = f4dd(__ldg(sp + (site + (3u * r + col) * N)));
+          const cplx<dd> lo = f4dd(__ldg(sp + (site + (unsigned)(3 * pr + col) * N)));
+          h[col] = coefmadd_rt(cr, s, lo, up);
+        }
+        // the lower spin that takes h_r in this direction, and its coefficient
+        const int rl = (gperm(mu, 2) == (int)r) ? 2 : 3;
+        const int cl = gcoef(mu, rl);
+        const float4* L = lk + (unsigned)(((fwd ? p : q) * 4 + mu) * 9) * (unsigned)g.Vh + (unsigned)(fwd ? cb : ycb);
+        const float cs = fwd ? 1.f : -1.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          cplx<dd> u[3];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const unsigned k = fwd ? (unsigned)(3 * i + j) : (unsigned)(3 * j + i);
+            const float4 qv = __ldg(L + k * (unsigned)g.Vh);
+            u[j] = mk<dd>(dd(qv.x, qv.z), dd_scale2(cs, dd(qv.y, qv.w)));  // U or U^dagger entry
+          }
+          cplx<dd> uh = cmul<dd>(u[0], h[0]);
+          uh = cmadd<dd>(uh, u[1], h[1]);
+          uh = cmadd<dd>(uh, u[2], h[2]);
+          float4& m = acc[i * bs];
+          m = ddf4(add<dd>(f4dd(m), uh));
+          float4& ml = acc[(3 + 3 * (rl - 2) + i) * bs];
+          ml = ddf4(coefmadd_rt(cl, s, uh, f4dd(ml)));
+        }
+      }
+    }
+    __syncwarp();  // the partner's accumulators are visible
+    ddc w[6];
+    if (active) {
+      const float4* mine = reinterpret_cast<const float4*>(smem_d) + t;
+      const float4* other = reinterpret_cast<const float4*>(smem_d) + (t ^ 1u);
+      if (r == 0) {  // spins 0 and 1: own upper sums and the partner's
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          w[i] = f4dd(mine[i * bs]);
+          w[3 + i] = f4dd(other[i * bs]);
+        }
+      } else {  // spins 2 and 3: thread 0's partial plus thread 1's
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = add<dd>(f4dd(other[(3 + k) * bs]), f4dd(mine[(3 + k) * bs]));
+      }
+    }
+    __syncwarp();  // both halves read before the next tile overwrites
+    if (active) {
+      const unsigned b = r;
+      if (a.l1.kind != LOC_NONE) local_half_dd(a.l1, g.Vh, p, cb, (int)b, w);
+      if (a.c1 != 1.0) {
+        const dd c1(a.c1);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          nrm<dd>(w[k]);
+          w[k] = scl<dd>(c1, w[k]);
+        }
+      }
+      const float4* Xp = reinterpret_cast<const float4*>(a.X);
+      if (Xp) {
+        ddc xv[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xv[k] = f4dd(__ldg(Xp + ((unsigned)n + (6u * b + k) * N)));
+        if (a.l2.kind != LOC_NONE) local_half_dd(a.l2, g.Vh, p, cb, (int)b, xv);
+        const dd c2(a.c2);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = mk<dd>(fma(c2, xv[k].x, w[k].x), fma(c2, xv[k].y, w[k].y));
+      }
+      float4* out = reinterpret_cast<float4*>(a.out);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) out[(unsigned)n + (6u * b + k) * N] = ddf4(w[k]);
+      if (a.red) {
+        double vr = 0, vi = 0;
+        dd sr = rzero<dd>(), si = rzero<dd>();
+        if (a.red == 1) {
+          const float4* Yp = reinterpret_cast<const float4*>(a.Y);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            ddc yv = f4dd(__ldg(Yp + ((unsigned)n + (6u * b + k) * N)));
+            ddc wk = w[k];
+            nrm<dd>(yv);
+            nrm<dd>(wk);
+            sr = fma(yv.x, wk.x, sr);
+            sr = fma(yv.y, wk.y, sr);
+            si = fma(yv.x, wk.y, si);
+            si = fma(-yv.y, wk.x, si);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            ddc wk = w[k];
+            nrm<dd>(wk);
+            sr = fma(wk.x, wk.x, sr);
+            sr = fma(wk.y, wk.y, sr);
+          }
+        }
+        vr = (double)sr;
+        vi = (double)si;
+        red_re += vr;
+        red_im += vi;
+      }
+    }
+    tile += gridDim.x;
+    if (LOOP) __syncthreads();
+  } while (LOOP && tile < ntiles);
+  if (a.red) {
+    double* sm = smem_d + (size_t)kDD2Acc * bs * 2;  // after the accumulators
+    block_reduce_finalize(a.ra, red_re, red_im, 1, 1, 1, sm);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host-side launcher
 // ---------------------------------------------------------------------------
 static int sm_count() {
@@ -792,8 +1014,35 @@ static cudaError_t launch_hop5t(const DslashArgs& a, cudaStream_t st) {
   return loop ? launch_hop5t_tl<LK, true>(a, bd, st) : launch_hop5t_tl<LK, false>(a, bd, st);
 }
 
+// the two-threads-per-site double-float hop (one rhs, per-thread epilogue)
+static size_t dd2_smem(int bd) { return (size_t)kDD2Acc * 16 * bd + 2 * 8 * (size_t)bd; }
+template <bool LOOP>
+static cudaError_t launch_dd2_tl(const DslashArgs& a, cudaStream_t st) {
+  const int bd = 256, sites = bd / 2;
+  const long long ntiles = (a.g.N + sites - 1) / sites;
+  const size_t sm = dd2_smem(bd);
+  auto k = dslash_dd2_kernel<LOOP>;
+  const int res = resident_blocks((const void*)k, bd, sm);
+  const long long nb = a.red ? reduce_grid(ntiles, 1, res) : ntiles;
+  k<<<(unsigned)nb, bd, sm, st>>>(a);
+  return cudaGetLastError();
+}
+static cudaError_t launch_dd2(const DslashArgs& a, cudaStream_t st) {
+  const long long ntiles = (a.g.N + 127) / 128;
+  const int res = resident_blocks((const void*)dslash_dd2_kernel<true>, 256, dd2_smem(256));
+  const bool loop = a.red && reduce_grid(ntiles, 1, res) < ntiles;
+  return loop ? launch_dd2_tl<true>(a, st) : launch_dd2_tl<false>(a, st);
+}
+static bool dd2_enabled();
+
 template <int P, int LS, int LK>
 static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
+  // the pure hop (no site-local term, no X, no reduction) of one rhs: two
+  // threads per site measured faster there (12.34 -> 11.55 ms on the
+  // reference's Dhop benchmark); with the clover epilogue it was slower
+  // (0.328 -> 0.345 ms per launch at 32^4), so the CG launches keep one thread
+  if (P == PDD && LK != LOC_SMAT && a.g.nrhs == 1 && a.l1.kind == LOC_NONE && !a.X && !a.red && dd2_enabled())
+    return launch_dd2(a, st);
   const int bd = pick_bd(a.bd, a.g.N5);
   if (bd <= 0) return cudaErrorInvalidValue;
   const long long ntiles = (a.g.N + bd - 1) / bd;
@@ -809,6 +1058,14 @@ static cudaError_t launch_t(const DslashArgs& a, cudaStream_t st) {
 static bool hop5_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("GBF_HOP5");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+// GBF_DD2=0 selects the one-thread-per-site double-float hop everywhere
+static bool dd2_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBF_DD2");
     return !(e && e[0] == '0');
   }();
   return on;
