@@ -72,8 +72,7 @@ __device__ __forceinline__ void site_dot_r(const cplx<R> (&a)[12], const cplx<R>
 // the block is staged in shared memory, so each B site is read from memory
 // once.
 template <int P>
-__global__ void __launch_bounds__(256) gram_kernel(const Geo g, const void* A, const void* B, double2* partial,
-                                                   unsigned* counter, double2* out) {
+__global__ void __launch_bounds__(256) gram_kernel(const Geo g, const void* A, const void* B, double2* partial) {
   using R = typename SpinorT<P>::R;
   using V = cplx<R>;
   extern __shared__ __align__(16) double sm_d[];  // [2k][bd] partials, then the [24][bd] tile, both R
@@ -123,29 +122,6 @@ __global__ void __launch_bounds__(256) gram_kernel(const Geo g, const void* A, c
       }
     partial[(size_t)blockIdx.x * k * k + q] = make_double2(re, im);
   }
-  __threadfence();
-  __syncthreads();
-  __shared__ int s_last;
-  if (t == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  // full warp w sums entries q = w, w + nw, ...: lane l adds blocks l,
-  // l + 32, ... in order, then a fixed shuffle tree (deterministic).  bd >= 129
-  // (block_size_for), so nw >= 4; a partial last warp takes no part.
-  const int lane = t & 31, nw = bd >> 5;
-  for (int q = t >> 5; q < k * k && (t >> 5) < nw; q += nw) {
-    double re = 0.0, im = 0.0;
-    for (unsigned b = lane; b < gridDim.x; b += 32) {
-      const double2 v = __ldcg(partial + (size_t)b * k * k + q);
-      re += v.x;
-      im += v.y;
-    }
-    re = warp_sum(re);
-    im = warp_sum(im);
-    if (lane == 0) out[q] = make_double2(re, im);
-  }
-  if (t == 0) *counter = 0u;
 }
 
 // The same Gram matrix for FP32 / FP16 fields, register-tiled.  A tile of
@@ -620,18 +596,6 @@ cudaError_t launch_lincomb2(int P, const Geo& g, void* out1, const void* Y1, dou
   return cudaGetLastError();
 }
 
-template <int P>
-static cudaError_t launch_gram_t(const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
-                                 unsigned* counter, double2* out, int bd, cudaStream_t st) {
-  const size_t sm = (size_t)2 * g.nrhs * bd * ((P == P64 || P == PDD) ? 8 : 4) + tile_bytes(P, bd);
-  auto k = gram_kernel<P>;
-  const int res = resident_blocks((const void*)k, bd, sm);
-  long long nb = reduce_grid((g.N + bd - 1) / bd, g.nrhs, res);
-  if (nb > max_blocks) nb = max_blocks;
-  k<<<(unsigned)nb, bd, sm, st>>>(g, A, B, partial, counter, out);
-  return cudaGetLastError();
-}
-
 // Sum of the [block][k*k] Gram partials: one block of 256 threads per entry
 // q, its threads take blocks b = t, t + 256, ... in order and a fixed
 // shuffle tree adds them (deterministic; many blocks share the work instead
@@ -648,6 +612,21 @@ __global__ void __launch_bounds__(256) gram_finalize_kernel(const double2* parti
   const double2 r = block_sum_shfl(re, im, sm);
   if (t == 0) out[q] = r;
 }
+
+template <int P>
+static cudaError_t launch_gram_t(const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
+                                 unsigned* counter, double2* out, int bd, cudaStream_t st) {
+  const size_t sm = (size_t)2 * g.nrhs * bd * ((P == P64 || P == PDD) ? 8 : 4) + tile_bytes(P, bd);
+  auto k = gram_kernel<P>;
+  const int res = resident_blocks((const void*)k, bd, sm);
+  long long nb = reduce_grid((g.N + bd - 1) / bd, g.nrhs, res);
+  if (nb > max_blocks) nb = max_blocks;
+  (void)counter;
+  k<<<(unsigned)nb, bd, sm, st>>>(g, A, B, partial);
+  gram_finalize_kernel<<<(unsigned)(g.nrhs * g.nrhs), 256, 0, st>>>(partial, (int)nb, g.nrhs * g.nrhs, out);
+  return cudaGetLastError();
+}
+
 
 template <int P, int T>
 static cudaError_t launch_gram_tiled(const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
@@ -693,11 +672,8 @@ static cudaError_t launch_gram_tiled_k(const Geo& g, const void* A, const void* 
   return launch_gram_tiled<P, 4>(g, A, B, partial, max_blocks, counter, out, bd, st);
 }
 
-// kernels one launch_gram issues (the FP32 / FP16 path adds the finalisation)
-int gram_launches(int P, const Geo& g) {
-  const int bd = block_size_for(g.N5, LOC_NONE);
-  return ((P == P32 || P == P16) && bd > 0 && bd % 16 == 0) ? 2 : 1;
-}
+// kernels one launch_gram issues: the partial sums and their finalisation
+int gram_launches(int, const Geo&) { return 2; }
 
 cudaError_t launch_gram(int P, const Geo& g, const void* A, const void* B, double2* partial, long long max_blocks,
                         unsigned* counter, double2* out, cudaStream_t st) {
