@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--profile-next", action="store_true",
                     help="profiling case of the kernels beyond the hot path: mode matrix, chiral shift, slice copy, "
                          "multi-shift update, block-CG Gram and linear combination (a few GB on the device)")
+    ap.add_argument("--profile-dhop", action="store_true",
+                    help="profiling case: the reference's Dhop benchmark on --dims (default 64,32,32,8), Ls 12, "
+                         "--profile-precision only, 20 applications")
     ap.add_argument("--profile-mobius", action="store_true",
                     help="profiling case: FP32 mobius 12^3x24 Ls 12 with 12 packed rhs, 12 CG iterations")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "next", "dslash"],
@@ -420,7 +423,7 @@ DHOP_PUBLISHED = {"single": {"gflops": 11325.46, "eff_gbs": 7824.86},
                   "hardware": "4x A100-SXM4-40GB (one JUWELS Booster node)"}
 
 
-def dwf_dhop_benchmark(reps=None):
+def dwf_dhop_benchmark(reps=None, dims=None, precisions=("single", "double_float", "double")):
     """The reference's headline benchmark (benchmarks/dslash.py) on one GPU:
     Mobius (mass 0.08, M5 1.8, b 1.5, c 0.5, Ls 12, periodic) Dhop on the
     full 5D field of a 64.32.32.32 lattice, N applications after 5 warm-up
@@ -434,7 +437,7 @@ def dwf_dhop_benchmark(reps=None):
     import gpt_gb300 as g
 
     L = g.load()
-    dims, Ls = [64, 32, 32, 32], 12
+    dims, Ls = dims or [64, 32, 32, 32], 12
     reps = reps or {"single": 1000, "double": 50, "double_float": 200}
     grid = g.grid(dims, g.double)
     U = g.qcd.gauge.random_su3_device(grid, 0.5, 777)
@@ -442,10 +445,12 @@ def dwf_dhop_benchmark(reps=None):
     V = grid.gsites
     sites = V * Ls
     stream = torch.cuda.current_stream()
-    out = {"workload": "mobius Dhop, full 5D field, 64.32.32.32 Ls 12 (benchmarks/dslash.py)",
+    out = {"workload": "mobius Dhop, full 5D field, %s Ls 12 (benchmarks/dslash.py)" % ".".join(map(str, dims)),
            "published_reference": DHOP_PUBLISHED}
     for name, prec, sb, lb in (("single", g.single, 96, 48), ("double_float", g.double_float, 192, 144),
-                               ("double", g.double, 192, 144)):
+                               ("double", g.double, 192, 144), ("half", g.half, 52, 48)):
+        if name not in precisions:
+            continue
         op = g.qcd.fermion.mobius(U, params)
         op = op if prec is g.double else op.converted(prec)
         src, dst = op.F_lattice(), op.F_lattice()
@@ -464,17 +469,28 @@ def dwf_dhop_benchmark(reps=None):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / n
-        wbytes = 8 if prec is not g.single else 4
+        wbytes = {"single": 4, "half": 2}.get(name, 8)
         eff = (8 * 2 * 4 * 3 + 8 * 2 * 9 / Ls + 2 * 4 * 3) * wbytes * sites
         alg = (sb + sb + 8 * lb / Ls) * sites
         r = {"applications": n, "ms_per_application": ms, "gflops": 1320.0 * sites / (ms / 1000.0) / 1e9,
              "eff_gbs_reference_model": eff / (ms / 1000.0) / 1e9, "algorithmic_gbs": alg / (ms / 1000.0) / 1e9}
         pub = DHOP_PUBLISHED.get("double" if name == "double_float" else name)
-        r["gflops_over_published_node"] = r["gflops"] / pub["gflops"]
+        if pub:
+            r["gflops_over_published_node"] = r["gflops"] / pub["gflops"]
         out[name] = r
         del op, src, dst
         torch.cuda.empty_cache()
     return out
+
+
+def run_profile_dhop(args):
+    """--profile-dhop: the Dhop benchmark's operator on a smaller lattice (by
+    default 64.32.32.8, the benchmark's x3 slices with an eighth of its
+    volume), one precision, 5 warm-up and 20 timed applications."""
+    dims = [int(x) for x in args.dims.split(",")] if args.dims else [64, 32, 32, 8]
+    r = dwf_dhop_benchmark({args.profile_precision: 20}, dims, (args.profile_precision,))
+    print(json.dumps({"workload": r["workload"], args.profile_precision: r[args.profile_precision]}), flush=True)
+    return 0
 
 
 def run_dslash_bench(args):
@@ -1337,6 +1353,8 @@ def main():
         return run_profile_case(args, dims)
     if args.profile_mobius:
         return run_profile_mobius(args)
+    if args.profile_dhop:
+        return run_profile_dhop(args)
     if args.profile_next:
         return run_profile_next(args)
     if args.impl != "reference" and args.config == "c1":

@@ -16,6 +16,8 @@
 // Roofline: HBM-bound in FP32/FP16 (per output site: 8 neighbour spinors that
 // the L2 mostly serves once, 8 links, 1 output); FP64 is bound by the FP64
 // pipe on GB300 (about 1.2 TFLOP/s measured).
+#include <array>
+#include <cstdio>
 #include <cstdlib>
 #include <map>
 #include <mutex>
@@ -307,8 +309,20 @@ __host__ __device__ inline size_t hop5_extra_smem(int S) {
 #define GBF_HOP5_MINB 3
 #endif
 
+// Order of the hop5 tiles.  lbx < 0: a tile is S consecutive checkerboard
+// sites, and with slabT > 0 the (x2, x3) planes are visited slab by slab
+// (slabT planes in x2, x3 slowest within a slab), so that a plane's x3
+// neighbours are read while they are still in L2.  lbx >= 0: a tile is a
+// brick of 2^lbx x 2^lby x 2^lbz x 2^lbt sites (x0/2, x1, x2, x3), whose
+// neighbours in all four directions largely coincide (L1 reuse inside the
+// block), and the bricks run x0 fastest within slabs of slabT planes in x2.
+struct Hop5Order {
+  int lbx, lby, lbz, lbt, slabT;
+};
+
 template <int P, int LK, bool LOOP>
-__global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashArgs a, unsigned epi_off16, int log2S) {
+__global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashArgs a, unsigned epi_off16, int log2S,
+                                                                   const Hop5Order ord) {
   using R = float;
   using V = float2;
   extern __shared__ __align__(16) double smem_d[];
@@ -317,18 +331,45 @@ __global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashAr
   const int p = a.out_parity, q = 1 - p;
   const unsigned t = threadIdx.x, bd = blockDim.x;
   const unsigned S = 1u << log2S;
+  constexpr unsigned kStride = kHop5LinkStride;
   float4* lsm = reinterpret_cast<float4*>(smem_d) + epi_off16;
-  int* nbs = reinterpret_cast<int*>(lsm + S * kHop5LinkStride);
+  int* nbs = reinterpret_cast<int*>(lsm + S * kStride);
   const unsigned j = g.fN5.div(t);  // 4D site of this thread within the tile
   const unsigned i5 = t - j * (unsigned)g.N5;
   double red_re = 0, red_im = 0;
   const long long ntiles = (g.N + bd - 1) / bd;
   long long tile = blockIdx.x;
   do {
-    const int cb0 = (int)(tile << log2S);
+    int cb0 = (int)(tile << log2S);
+    unsigned o0 = 0, o1 = 0, o2 = 0, o3 = 0;  // brick origin
+    if (ord.lbx >= 0) {
+      unsigned r = (unsigned)tile, qq;
+      const unsigned n0 = (unsigned)g.Lh0 >> ord.lbx, n1 = (unsigned)g.L[1] >> ord.lby;
+      const unsigned n2 = (unsigned)ord.slabT >> ord.lbz, n3 = (unsigned)g.L[3] >> ord.lbt;
+      qq = r / n0; o0 = (r - qq * n0) << ord.lbx; r = qq;
+      qq = r / n1; o1 = (r - qq * n1) << ord.lby; r = qq;
+      qq = r / n2; o2 = (r - qq * n2) << ord.lbz; r = qq;
+      qq = r / n3; o3 = (r - qq * n3) << ord.lbt;
+      o2 += qq * (unsigned)ord.slabT;
+    } else if (ord.slabT) {
+      const unsigned pt = (unsigned)(g.Lh0 * g.L[1]) >> log2S;  // tiles per (x2, x3) plane
+      const unsigned tp = (unsigned)tile / pt, w = (unsigned)tile - tp * pt;
+      const unsigned r = tp / (unsigned)ord.slabT, x2 = tp - r * (unsigned)ord.slabT;
+      const unsigned b = r / (unsigned)g.L[3], x3 = r - b * (unsigned)g.L[3];
+      cb0 = (int)(((b * (unsigned)ord.slabT + x2 + (unsigned)g.L[2] * x3) * pt + w) << log2S);
+    }
+    auto site_of = [&](unsigned jj) -> int {
+      if (ord.lbx < 0) return cb0 + (int)jj;
+      const unsigned j0 = jj & ((1u << ord.lbx) - 1u);
+      jj >>= ord.lbx;
+      const unsigned j1 = jj & ((1u << ord.lby) - 1u);
+      jj >>= ord.lby;
+      const unsigned j2 = jj & ((1u << ord.lbz) - 1u), j3 = jj >> ord.lbz;
+      return (int)((o0 + j0) + (unsigned)g.Lh0 * ((o1 + j1) + (unsigned)g.L[1] * ((o2 + j2) + (unsigned)g.L[2] * (o3 + j3))));
+    };
     // ---- neighbour indices of the S sites (bit 31: unused) ----
     for (unsigned idx = t; idx < 8 * S; idx += bd) {
-      const int jj = idx >> 3, d = idx & 7, cbj = cb0 + jj;
+      const int jj = idx >> 3, d = idx & 7, cbj = site_of(jj);
       int ycb = 0;
       if (cbj < g.Vh) {
         const Coord c = cb_coords(g, cbj, p);
@@ -349,7 +390,7 @@ __global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashAr
       for (unsigned idx = t; idx < total; idx += bd) {
         const unsigned jj = idx & (S - 1), dk = idx >> log2S;
         const unsigned d = dk / 9u, k = dk - 9u * d;
-        const int cbj = cb0 + (int)jj;
+        const int cbj = site_of(jj);
         if (cbj >= g.Vh) continue;
         const int mu = d >> 1;
         const bool fwd = (d & 1) == 0;
@@ -361,12 +402,12 @@ __global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashAr
           kk = (k % 3u) * 3u + k / 3u;
           v.y = -v.y;
         }
-        *reinterpret_cast<float2*>(lf + (jj * kHop5LinkStride + d * 5u) * 4u + 2u * kk) = v;
+        *reinterpret_cast<float2*>(lf + (jj * kStride + d * 5u) * 4u + 2u * kk) = v;
       }
     }
     __syncthreads();
-    const long long n = tile * bd + t;
-    const int cb = cb0 + (int)j;
+    const int cb = site_of(j);
+    const long long n = (long long)cb * g.N5 + i5;
     const bool active = cb < g.Vh;
     V res[12];
 #pragma unroll
@@ -374,7 +415,7 @@ __global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashAr
     if (active) {
       const R sf = (R)a.sgn;
       const int* nbj = nbs + j * 8;
-      const float4* lj = lsm + j * kHop5LinkStride;
+      const float4* lj = lsm + j * kStride;
 #pragma unroll
       for (int mu = 0; mu < 4; ++mu) {
 #pragma unroll
@@ -956,6 +997,60 @@ static cudaError_t launch_tl(const DslashArgs& a, cudaStream_t st) {
 }
 
 // hop5: the epilogue's shared memory first, then the links and indices
+// Order of the hop5 tiles for tiles of S 4D sites.  The brick is
+// min(S, 4) sites in x0/2 by the rest in x1 where those divide the lattice,
+// else S consecutive sites.  The slab depth T (x2 planes) is the largest
+// divisor of L2 below L2 (a multiple of the brick's x2 extent) whose three x3
+// steps (T planes each; input, output and X term) stay within 64 MB of L2;
+// no slabs when the whole field fits in 64 MB.  GBF_HOP5_SLAB=<T> forces T
+// (0: none); GBF_HOP5_BRICK=<b0,b1,b2,b3> forces the brick (0: consecutive
+// sites).
+static Hop5Order hop5_order(const DslashArgs& a, int S) {
+  static const int forced_slab = [] {
+    const char* e = std::getenv("GBF_HOP5_SLAB");
+    return e ? std::atoi(e) : -1;
+  }();
+  static const std::array<int, 4> forced_brick = [] {
+    std::array<int, 4> b{-1, -1, -1, -1};
+    const char* e = std::getenv("GBF_HOP5_BRICK");
+    if (e) {
+      if (std::sscanf(e, "%d,%d,%d,%d", &b[0], &b[1], &b[2], &b[3]) != 4) b = {0, 0, 0, 0};
+    }
+    return b;
+  }();
+  const Geo& g = a.g;
+  Hop5Order o{-1, 0, 0, 0, 0};
+  int br[4] = {S < 4 ? S : 4, S < 4 ? 1 : S / 4, 1, 1};
+  if (forced_brick[0] >= 0) {
+    for (int i = 0; i < 4; ++i) br[i] = forced_brick[i];
+  }
+  const int ext[4] = {g.Lh0, g.L[1], g.L[2], g.L[3]};
+  bool brick = br[0] > 0 && (long long)br[0] * br[1] * br[2] * br[3] == S;
+  for (int i = 0; i < 4 && brick; ++i) brick = br[i] > 0 && (br[i] & (br[i] - 1)) == 0 && ext[i] % br[i] == 0;
+  const long long P = (long long)g.Lh0 * g.L[1];
+  if (!brick && P % S) return o;
+  const int bz = brick ? br[2] : 1;
+  const double step = (double)P * g.N5 * 96.0 * (a.X ? 3 : 2);
+  int T = 0;
+  if (forced_slab >= 0) {
+    T = (forced_slab > 0 && forced_slab < g.L[2] && g.L[2] % forced_slab == 0 && forced_slab % bz == 0) ? forced_slab : 0;
+  } else if ((double)g.L[2] * g.L[3] * step > 64e6) {
+    for (int t = bz; t < g.L[2]; t += bz)
+      if (g.L[2] % t == 0 && 3.0 * t * step <= 64e6) T = t;
+  }
+  if (brick) {
+    int l[4];
+    for (int i = 0; i < 4; ++i) {
+      l[i] = 0;
+      while ((1 << l[i]) < br[i]) ++l[i];
+    }
+    o = Hop5Order{l[0], l[1], l[2], l[3], T ? T : g.L[2]};
+  } else {
+    o.slabT = T;
+  }
+  return o;
+}
+
 template <int P, int LK, bool LOOP>
 static cudaError_t launch_hop5_tl(const DslashArgs& a, int bd, cudaStream_t st) {
   const int S = bd / a.g.N5;
@@ -968,7 +1063,7 @@ static cudaError_t launch_hop5_tl(const DslashArgs& a, int bd, cudaStream_t st) 
   auto k = hop5_kernel<P, LK, LOOP>;
   const int res = resident_blocks((const void*)k, bd, sm);
   const long long nb = a.red ? reduce_grid(ntiles, a.g.nrhs, res) : ntiles;
-  k<<<(unsigned)nb, bd, sm, st>>>(a, off16, log2S);
+  k<<<(unsigned)nb, bd, sm, st>>>(a, off16, log2S, hop5_order(a, S));
   return cudaGetLastError();
 }
 
