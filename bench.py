@@ -908,8 +908,13 @@ def run_profile_case(args, dims):
     torch.cuda.synchronize()
     r = op._solve_eo2ne_cg(x, src, 1e-30, 12)
     torch.cuda.synchronize()
+    # the same solve once more with per-kernel-class timing (events around
+    # the launches: hop, site-local, vector kernels)
+    rp = op._solve_eo2ne_cg(x, src, 1e-30, 12, 0, 1)
+    torch.cuda.synchronize()
     print(json.dumps({"profile_case": f"wilson_clover {args.profile_precision} eo2_ne CG, 12 iterations", "lattice": dims,
-                      "iterations": r.iterations, "link_bytes": op.link_bytes()}))
+                      "iterations": r.iterations, "link_bytes": op.link_bytes(),
+                      "kernel_ms": list(rp.kernel_ms), "kernel_launches": list(rp.kernel_launches)}))
     return 0
 
 

@@ -167,6 +167,72 @@ template <> struct C2<dd> { using T = ddc; };
 template <> __device__ __forceinline__ dd rzero<dd>() { return dd(0.f, 0.f); }
 template <> __device__ __forceinline__ cplx<dd> cz<dd>() { return mk<dd>(dd(0.f, 0.f), dd(0.f, 0.f)); }
 
+// Two double-float numbers as lanes of FP32 pairs (fma.rn.f32x2 and
+// add.rn.f32x2 on sm_100 and later): value_k = h.k + l.k for k = x, y.  As a
+// complex double-float, x is the real and y the imaginary part, which is the
+// float4 storage (x.h, y.h, x.l, y.l) of double-float fields and links, so a
+// 16-byte load is a pdd.  Every operation is the lane-wise form of the
+// scalar one above (the same steps in the same order), so the results equal
+// the scalar code's while the FP32 pipe is issued half the instructions.
+struct pdd {
+  float2 h, l;
+};
+__device__ __forceinline__ pdd pdd_ld(const float4 q) { return pdd{make_float2(q.x, q.y), make_float2(q.z, q.w)}; }
+__device__ __forceinline__ float4 pdd_st(const pdd a) { return make_float4(a.h.x, a.h.y, a.l.x, a.l.y); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, neg2(a));
+  e = __fadd2_rn(__fadd2_rn(a, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(b, neg2(bb)));
+}
+__device__ __forceinline__ pdd fast_two_sum2(float2 a, float2 b) {
+  const float2 s = __fadd2_rn(a, b);
+  return pdd{s, __fadd2_rn(b, neg2(__fadd2_rn(s, neg2(a))))};
+}
+// a + b
+__device__ __forceinline__ pdd pdd_add(pdd a, pdd b) {
+  float2 s, e;
+  two_sum2(a.h, b.h, s, e);
+  return fast_two_sum2(s, __fadd2_rn(e, __fadd2_rn(a.l, b.l)));
+}
+// f a + c for a double-float scalar f (as fma(dd, dd, dd); c = 0 gives the
+// un-normalised product, as cmul)
+__device__ __forceinline__ pdd pdd_fma_s(dd f, pdd a, pdd c) {
+  const float2 fh = make_float2(f.h, f.h), fl = make_float2(f.l, f.l);
+  const float2 p = __fmul2_rn(fh, a.h);
+  float2 e = __ffma2_rn(fh, a.h, neg2(p));
+  e = __ffma2_rn(fh, a.l, e);
+  e = __ffma2_rn(fl, a.h, e);
+  float2 s, t;
+  two_sum2(p, c.h, s, t);
+#ifdef GBF_DD_RENORM
+  return fast_two_sum2(s, __fadd2_rn(t, __fadd2_rn(e, c.l)));
+#else
+  return pdd{s, __fadd2_rn(t, __fadd2_rn(e, c.l))};
+#endif
+}
+// f a: fma with c = 0 without the two-sum with zero (equal up to the sign
+// of a zero low word)
+__device__ __forceinline__ pdd pdd_mul_s(dd f, pdd a) {
+  const float2 fh = make_float2(f.h, f.h), fl = make_float2(f.l, f.l);
+  const float2 p = __fmul2_rn(fh, a.h);
+  float2 e = __ffma2_rn(fh, a.h, neg2(p));
+  e = __ffma2_rn(fh, a.l, e);
+  e = __ffma2_rn(fl, a.h, e);
+  return pdd{p, e};
+}
+// i a
+__device__ __forceinline__ pdd pdd_i(pdd a) { return pdd{make_float2(-a.h.y, a.h.x), make_float2(-a.l.y, a.l.x)}; }
+__device__ __forceinline__ pdd pdd_nrm(pdd a) { return fast_two_sum2(a.h, a.l); }
+// a + s coef v with run-time coefficient code and sign (as coefmadd_rt)
+__device__ __forceinline__ pdd pdd_coefmadd_rt(int code, float s, pdd v, pdd a) {
+  const bool im = code >= 2;
+  const float sg = (code == 1 || code == 3) ? -s : s;
+  const pdd w = im ? pdd_i(v) : v;
+  const float2 f = make_float2(sg, sg);
+  return pdd_add(a, pdd{__fmul2_rn(f, w.h), __fmul2_rn(f, w.l)});
+}
+
 // Normalise an fma result before it is stored or used as a factor: with
 // cancellation in the un-normalised pair |l| can exceed |h|, and a product
 // (which drops l_a l_b) would then be wrong.  No-op for FP32 / FP64.

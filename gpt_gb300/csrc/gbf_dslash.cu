@@ -160,6 +160,59 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
         const int ycb = cb_index(g, y);
         const unsigned site = (unsigned)ycb * (unsigned)g.N5 + i5;
         const float s = fwd ? a.sgn : -a.sgn;
+#ifndef GBF_DD_SCALAR
+        // lane-paired form (pdd): u h = Re(u) h + Im(u) (i h), and the
+        // backward term's conj(u) negates Im(u)
+        {
+          const float4* sp = reinterpret_cast<const float4*>(a.in);
+          const unsigned N = (unsigned)g.N;
+          pdd h[2][3];
+#pragma unroll
+          for (int r = 0; r < 2; ++r) {
+            const int pr = gperm(mu, r), cr = gcoef(mu, r);
+#pragma unroll
+            for (int col = 0; col < 3; ++col) {
+              const pdd up = pdd_ld(__ldg(sp + (site + (unsigned)(3 * r + col) * N)));
+              const pdd lo = pdd_ld(__ldg(sp + (site + (unsigned)(3 * pr + col) * N)));
+              h[r][col] = pdd_coefmadd_rt(cr, s, lo, up);
+            }
+          }
+          const float4* L = reinterpret_cast<const float4*>(a.links) +
+                            (unsigned)(((fwd ? p : q) * 4 + mu) * 9) * (unsigned)g.Vh + (unsigned)(fwd ? cb : ycb);
+          const float cs = fwd ? 1.f : -1.f;
+          pdd uh[2][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const unsigned k = fwd ? (unsigned)(3 * i + j) : (unsigned)(3 * j + i);
+              const float4 qv = __ldg(L + k * (unsigned)g.Vh);
+              const dd ux(qv.x, qv.z), uy = dd_scale2(cs, dd(qv.y, qv.w));
+#pragma unroll
+              for (int r = 0; r < 2; ++r) {
+                uh[r][i] = j == 0 ? pdd_mul_s(ux, h[r][j]) : pdd_fma_s(ux, h[r][j], uh[r][i]);
+                uh[r][i] = pdd_fma_s(uy, pdd_i(h[r][j]), uh[r][i]);
+              }
+            }
+#pragma unroll
+          for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              float4& m = acc[(3 * r + i) * bs];
+              m = pdd_st(pdd_add(pdd_ld(m), uh[r][i]));
+            }
+#pragma unroll
+          for (int r = 2; r < 4; ++r) {
+            const bool first = gperm(mu, r) == 0;
+            const int cr = gcoef(mu, r);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              float4& m = acc[(3 * r + i) * bs];
+              m = pdd_st(pdd_coefmadd_rt(cr, s, first ? uh[0][i] : uh[1][i], pdd_ld(m)));
+            }
+          }
+        }
+#else
         cplx<dd> h[2][3];
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
@@ -201,6 +254,7 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
             m = make_float4(v.x.h, v.y.h, v.x.l, v.y.l);
           }
         }
+#endif
       }
 #pragma unroll
       for (int k = 0; k < 12; ++k) {
@@ -791,6 +845,41 @@ __global__ void __launch_bounds__(256, GBF_DD2_MINB) dslash_dd2_kernel(const Dsl
         const unsigned site = (unsigned)ycb * (unsigned)g.N5 + i5;
         const float s = fwd ? a.sgn : -a.sgn;
         const int pr = gperm(mu, (int)r), cr = gcoef(mu, (int)r);
+#ifndef GBF_DD_SCALAR
+        {
+          // lane-paired form: a complex double-float is one pdd, u h is
+          // Re(u) h + Im(u) (i h), two lane-wise fmas per link entry
+          pdd h[3], ih[3];
+#pragma unroll
+          for (int col = 0; col < 3; ++col) {
+            const pdd up = pdd_ld(__ldg(sp + (site + (3u * r + col) * N)));
+            const pdd lo = pdd_ld(__ldg(sp + (site + (unsigned)(3 * pr + col) * N)));
+            h[col] = pdd_coefmadd_rt(cr, s, lo, up);
+            ih[col] = pdd_i(h[col]);
+          }
+          const int rl = (gperm(mu, 2) == (int)r) ? 2 : 3;
+          const int cl = gcoef(mu, rl);
+          const float4* L = lk + (unsigned)(((fwd ? p : q) * 4 + mu) * 9) * (unsigned)g.Vh + (unsigned)(fwd ? cb : ycb);
+          const float cs = fwd ? 1.f : -1.f;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            pdd uh;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const unsigned k = fwd ? (unsigned)(3 * i + j) : (unsigned)(3 * j + i);
+              const float4 qv = __ldg(L + k * (unsigned)g.Vh);
+              const dd ux(qv.x, qv.z), uy = dd_scale2(cs, dd(qv.y, qv.w));  // U or U^dagger entry
+              uh = j == 0 ? pdd_mul_s(ux, h[j]) : pdd_fma_s(ux, h[j], uh);
+              uh = pdd_fma_s(uy, ih[j], uh);
+            }
+            // (the sums leave pdd_add normalised)
+            float4& m = acc[i * bs];
+            m = pdd_st(pdd_add(pdd_ld(m), uh));
+            float4& ml = acc[(3 + 3 * (rl - 2) + i) * bs];
+            ml = pdd_st(pdd_coefmadd_rt(cl, s, uh, pdd_ld(ml)));
+          }
+        }
+#else
         cplx<dd> h[3];
 #pragma unroll
         for (int col = 0; col < 3; ++col) {
@@ -820,6 +909,7 @@ __global__ void __launch_bounds__(256, GBF_DD2_MINB) dslash_dd2_kernel(const Dsl
           float4& ml = acc[(3 + 3 * (rl - 2) + i) * bs];
           ml = ddf4(coefmadd_rt(cl, s, uh, f4dd(ml)));
         }
+#endif
       }
     }
     __syncwarp();  // the partner's accumulators are visible
