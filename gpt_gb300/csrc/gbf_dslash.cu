@@ -359,8 +359,15 @@ __host__ __device__ inline size_t hop5_extra_smem(int S) {
   return (size_t)S * kHop5LinkStride * 16 + (size_t)S * 8 * 4;
 }
 
+// Resident blocks per SM the hop5 kernels are compiled for: 3 (80
+// registers) with the s-matrix epilogue or a looping reduction, 4 (64
+// registers) otherwise, the faster of each measured on GB300 (more warps
+// hide the neighbour loads; the other two spill at 64)
 #ifndef GBF_HOP5_MINB
 #define GBF_HOP5_MINB 3
+#endif
+#ifndef GBF_HOP5_MINB_THREAD
+#define GBF_HOP5_MINB_THREAD 4
 #endif
 
 // Order of the hop5 tiles.  lbx < 0: a tile is S consecutive checkerboard
@@ -375,7 +382,8 @@ struct Hop5Order {
 };
 
 template <int P, int LK, bool LOOP>
-__global__ void __launch_bounds__(256, GBF_HOP5_MINB) hop5_kernel(const DslashArgs a, unsigned epi_off16, int log2S,
+__global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB : GBF_HOP5_MINB_THREAD)
+    hop5_kernel(const DslashArgs a, unsigned epi_off16, int log2S,
                                                                    const Hop5Order ord) {
   using R = float;
   using V = float2;
