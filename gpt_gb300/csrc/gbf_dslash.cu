@@ -444,33 +444,67 @@ __global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB 
       nbs[idx] = ycb;
     }
     __syncthreads();
-    // ---- links: component k of link d of site jj, jj fastest (coalesced) ----
+    const int cb = site_of(j);
+    const long long n = (long long)cb * g.N5 + i5;
+    const bool active = cb < g.Vh;
+    // ---- links: component k of link d of site jj, jj fastest (coalesced).
+    // Each thread's link entries (at most 9: 72 S entries over S N5 >= 8 S
+    // threads) are requested, then (one-pass launches with a per-thread
+    // epilogue) its first neighbour spinor, and only then are the links
+    // stored, so the spinor load overlaps the link latency.  The looping and
+    // s-matrix launches skip the early load (measured slower there).
+    constexpr bool kEarly = !LOOP && LK != LOC_SMAT;
+    V psi0[12];
     {
       const float2* L2 = reinterpret_cast<const float2*>(a.links);
       float* lf = reinterpret_cast<float*>(lsm);
       const unsigned total = 72u * S;
-      for (unsigned idx = t; idx < total; idx += bd) {
-        const unsigned jj = idx & (S - 1), dk = idx >> log2S;
-        const unsigned d = dk / 9u, k = dk - 9u * d;
+      auto link_src = [&](unsigned idx, unsigned& jj, unsigned& d, unsigned& k) -> const float2* {
+        jj = idx & (S - 1);
+        const unsigned dk = idx >> log2S;
+        d = dk / 9u;
+        k = dk - 9u * d;
         const int cbj = site_of(jj);
-        if (cbj >= g.Vh) continue;
+        if (cbj >= g.Vh) return nullptr;
         const int mu = d >> 1;
         const bool fwd = (d & 1) == 0;
         const int site = fwd ? cbj : nbs[jj * 8 + d];
         const int par = fwd ? p : q;
-        float2 v = __ldg(L2 + ((unsigned)((par * 4 + mu) * 9) + k) * (unsigned)g.Vh + (unsigned)site);
+        return L2 + ((unsigned)((par * 4 + mu) * 9) + k) * (unsigned)g.Vh + (unsigned)site;
+      };
+      auto link_store = [&](unsigned jj, unsigned d, unsigned k, float2 v) {
         unsigned kk = k;
-        if (!fwd) {  // U^dagger: (i, j) <- conj (j, i)
+        if (d & 1) {  // U^dagger: (i, j) <- conj (j, i)
           kk = (k % 3u) * 3u + k / 3u;
           v.y = -v.y;
         }
         *reinterpret_cast<float2*>(lf + (jj * kStride + d * 5u) * 4u + 2u * kk) = v;
+      };
+      if constexpr (kEarly) {
+        float2 lv[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          unsigned jj, d, k;
+          const unsigned idx = t + (unsigned)c * bd;
+          const float2* src = idx < total ? link_src(idx, jj, d, k) : nullptr;
+          lv[c] = src ? __ldg(src) : make_float2(0.f, 0.f);
+        }
+        if (active) load_spinor<P>(a.in, g.N, (unsigned)nbs[j * 8] * (unsigned)g.N5 + i5, psi0);
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          unsigned jj, d, k;
+          const unsigned idx = t + (unsigned)c * bd;
+          if (idx < total && link_src(idx, jj, d, k)) link_store(jj, d, k, lv[c]);
+        }
+      } else {
+        for (unsigned idx = t; idx < total; idx += bd) {
+          unsigned jj, d, k;
+          const float2* src = link_src(idx, jj, d, k);
+          if (src) link_store(jj, d, k, __ldg(src));
+        }
       }
     }
     __syncthreads();
-    const int cb = site_of(j);
-    const long long n = (long long)cb * g.N5 + i5;
-    const bool active = cb < g.Vh;
     V res[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) res[k] = cz<R>();
@@ -484,9 +518,13 @@ __global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB 
         for (int dir = 0; dir < 2; ++dir) {
           const int d = 2 * mu + dir;
           const bool fwd = dir == 0;
-          const unsigned ycb = (unsigned)nbj[d];
           V psi[12];
-          load_spinor<P>(a.in, g.N, ycb * (unsigned)g.N5 + i5, psi);
+          if (kEarly && d == 0) {
+#pragma unroll
+            for (int k = 0; k < 12; ++k) psi[k] = psi0[k];
+          } else {
+            load_spinor<P>(a.in, g.N, (unsigned)nbj[d] * (unsigned)g.N5 + i5, psi);
+          }
           const R s = fwd ? sf : -sf;
           V h[2][3];
 #pragma unroll
