@@ -355,8 +355,9 @@ __global__ void __launch_bounds__(256, (P == P64 ? 1 : P == PDD ? GBF_DSLASH_MIN
 // ---------------------------------------------------------------------------
 constexpr int kHop5LinkStride = 41;  // float4 per site (8 links x 5, +1 pad: site rows 4 banks apart)
 
+// links, neighbour indices and (hop5_kernel) the link offsets of the S sites
 __host__ __device__ inline size_t hop5_extra_smem(int S) {
-  return (size_t)S * kHop5LinkStride * 16 + (size_t)S * 8 * 4;
+  return (size_t)S * kHop5LinkStride * 16 + (size_t)S * 16 * 4;
 }
 
 // Resident blocks per SM the hop5 kernels are compiled for: 3 (80
@@ -429,10 +430,14 @@ __global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB 
       const unsigned j2 = jj & ((1u << ord.lbz) - 1u), j3 = jj >> ord.lbz;
       return (int)((o0 + j0) + (unsigned)g.Lh0 * ((o1 + j1) + (unsigned)g.L[1] * ((o2 + j2) + (unsigned)g.L[2] * (o3 + j3))));
     };
-    // ---- neighbour indices of the S sites (bit 31: unused) ----
+    // ---- neighbour indices of the S sites, and the offset of each site's
+    // link d in the link planes (fwd: U_mu(x) of parity p, bwd: U_mu(x - mu)
+    // of parity q; ~0u for a site past the end) ----
+    unsigned* loff = reinterpret_cast<unsigned*>(nbs + 8 * S);
     for (unsigned idx = t; idx < 8 * S; idx += bd) {
       const int jj = idx >> 3, d = idx & 7, cbj = site_of(jj);
       int ycb = 0;
+      unsigned lo = ~0u;
       if (cbj < g.Vh) {
         const Coord c = cb_coords(g, cbj, p);
         const int mu = d >> 1;
@@ -440,8 +445,11 @@ __global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB 
         if ((d & 1) == 0) y[mu] = (y[mu] == g.L[mu] - 1) ? 0 : y[mu] + 1;
         else y[mu] = (y[mu] == 0) ? g.L[mu] - 1 : y[mu] - 1;
         ycb = cb_index(g, y);
+        const bool fwd = (d & 1) == 0;
+        lo = (unsigned)(((fwd ? p : q) * 4 + mu) * 9) * (unsigned)g.Vh + (unsigned)(fwd ? cbj : ycb);
       }
       nbs[idx] = ycb;
+      loff[idx] = lo;
     }
     __syncthreads();
     const int cb = site_of(j);
@@ -464,13 +472,8 @@ __global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB 
         const unsigned dk = idx >> log2S;
         d = dk / 9u;
         k = dk - 9u * d;
-        const int cbj = site_of(jj);
-        if (cbj >= g.Vh) return nullptr;
-        const int mu = d >> 1;
-        const bool fwd = (d & 1) == 0;
-        const int site = fwd ? cbj : nbs[jj * 8 + d];
-        const int par = fwd ? p : q;
-        return L2 + ((unsigned)((par * 4 + mu) * 9) + k) * (unsigned)g.Vh + (unsigned)site;
+        const unsigned lo = loff[jj * 8 + d];
+        return lo == ~0u ? nullptr : L2 + (lo + k * (unsigned)g.Vh);
       };
       auto link_store = [&](unsigned jj, unsigned d, unsigned k, float2 v) {
         unsigned kk = k;
@@ -490,11 +493,14 @@ __global__ void __launch_bounds__(256, (LK == LOC_SMAT || LOOP) ? GBF_HOP5_MINB 
           lv[c] = src ? __ldg(src) : make_float2(0.f, 0.f);
         }
         if (active) load_spinor<P>(a.in, g.N, (unsigned)nbs[j * 8] * (unsigned)g.N5 + i5, psi0);
+        // (a site past the end gets zero links; it is inactive)
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
-          unsigned jj, d, k;
           const unsigned idx = t + (unsigned)c * bd;
-          if (idx < total && link_src(idx, jj, d, k)) link_store(jj, d, k, lv[c]);
+          if (idx < total) {
+            const unsigned jj = idx & (S - 1), dk = idx >> log2S, d = dk / 9u;
+            link_store(jj, d, dk - 9u * d, lv[c]);
+          }
         }
       } else {
         for (unsigned idx = t; idx < total; idx += bd) {
