@@ -426,8 +426,9 @@ DHOP_PUBLISHED = {"single": {"gflops": 11325.46, "eff_gbs": 7824.86},
 def dwf_dhop_benchmark(reps=None, dims=None, precisions=("single", "double_float", "double")):
     """The reference's headline benchmark (benchmarks/dslash.py) on one GPU:
     Mobius (mass 0.08, M5 1.8, b 1.5, c 0.5, Ls 12, periodic) Dhop on the
-    full 5D field of a 64.32.32.32 lattice, N applications after 5 warm-up
-    ones; flops = 1320 per 5D site and 'effective GB/s' = (8*2*4*3 +
+    full 5D field of a 64.32.32.32 lattice (or `dims`), N applications after
+    5 warm-up ones, in each of `precisions` (single, double_float, double,
+    half); flops = 1320 per 5D site and 'effective GB/s' = (8*2*4*3 +
     8*2*9/Ls + 2*4*3) reals per 5D site, the reference's models
     (dslash.py:54-61).  The algorithmic GB/s beside them counts each
     neighbour spinor once (L2 serves the eightfold reuse) and the links once
